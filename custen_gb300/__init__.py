@@ -1,0 +1,184 @@
+"""custen_gb300 -- GB300 (sm_103a) rebuild of the cuSten 2D stencil library: Python host side.
+
+The compute path is the in-tree shared library ``libcusten_gb300.so`` (CUDA kernels + C-ABI,
+``include/custen_gb300.h``). This module binds that C-ABI with ctypes and mirrors the reference's
+handle API (``cuStenCreate2D*`` / ``cuStenCompute2D*`` / ``cuStenSwap2D*`` / ``cuStenDestroy2D*``,
+cuSten/src/struct/cuSten_struct_functions.h and cuSten/src/kernels/stencil_kernels.h): a
+:class:`Stencil` object owns one 200-byte ``cuSten_t`` handle.
+
+There is no CPU fallback: if the shared library is missing, importing the compute API raises.
+Data arguments are device-accessible addresses (ints), or objects exposing ``data_ptr()``
+(torch tensors) or ``ctypes.data`` (numpy views of managed memory).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libcusten_gb300.so"
+
+# Variant codes (include/custen_gb300.h).
+XP, XNP, XPFUN, XNPFUN, YP, YNP, YPFUN, YNPFUN, XYP, XYNP, XYPFUN, XYNPFUN = range(12)
+VARIANT_NAMES = ["Xp", "Xnp", "XpFun", "XnpFun", "Yp", "Ynp", "YpFun", "YnpFun", "XYp", "XYnp", "XYpFun",
+                 "XYnpFun"]
+F64, F32 = 0, 1
+DEVICE, HOST = 0, 1
+HANDLE_BYTES = 200
+
+_lib = None
+
+
+class CustenError(RuntimeError):
+    pass
+
+
+def build() -> Path:
+    from . import buildlib
+    return buildlib.build()
+
+
+def lib() -> ctypes.CDLL:
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise CustenError(f"{LIB_PATH} is missing: run custen_gb300.build() (no CPU fallback exists)")
+        L = ctypes.CDLL(str(LIB_PATH))
+        vp, i, ull, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_size_t
+        L.custen_last_error.restype = ctypes.c_char_p
+        L.custen_kernel_launches.restype = ull
+        L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
+        L.custen_compute.argtypes = [vp, i]
+        L.custen_compute_on_stream.argtypes = [vp, i, vp]
+        L.custen_swap.argtypes = [vp, vp]
+        L.custen_destroy.argtypes = [vp]
+        L.custen_set_stream.argtypes = [vp, vp]
+        L.custen_handle_variant.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.custen_builtin_function.argtypes = [i, i, ctypes.POINTER(vp)]
+        for name in ("custen_malloc_managed", "custen_malloc_device", "custen_malloc_host"):
+            getattr(L, name).argtypes = [ctypes.POINTER(vp), sz]
+        L.custen_free.argtypes = [vp]
+        L.custen_free_host.argtypes = [vp]
+        L.custen_memcpy.argtypes = [vp, vp, sz]
+        L.custen_memset.argtypes = [vp, i, sz]
+        L.custen_set_device.argtypes = [i]
+        _lib = L
+    return _lib
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        raise CustenError(lib().custen_last_error().decode(errors="replace"))
+
+
+def addr(x) -> int | None:
+    """Device-accessible address of x (int, torch tensor, numpy array, ctypes object or None)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    if hasattr(x, "ctypes"):
+        return int(x.ctypes.data)
+    if isinstance(x, ctypes.c_void_p):
+        return x.value
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def builtin_function(fid: int, dtype: int = F64) -> int:
+    """Device address of one of the shipped Fun device functions (include/custen_gb300.h)."""
+    p = ctypes.c_void_p()
+    _check(lib().custen_builtin_function(fid, dtype, ctypes.byref(p)))
+    return int(p.value)
+
+
+def kernel_launches() -> int:
+    return int(lib().custen_kernel_launches())
+
+
+class Stencil:
+    """One cuSten handle. Mirrors cuStenCreate2D<variant> / Compute / Swap / Destroy.
+
+    Window geometry: H/L/R in x, V/T/B in y (X variants: V=1, T=B=0; Y variants: H=1, L=R=0).
+    ``ncoef`` defaults to the number the reference reads per Compute for the variant.
+    """
+
+    def __init__(self, variant: int, nx: int, ny: int, out, inp, coef, *, H=1, L=0, R=0, V=1, T=0, B=0,
+                 num_tiles=1, block_x=32, block_y=8, dtype=F64, device=0, ncoef=None, func=None):
+        self.variant, self.dtype = variant, dtype
+        self.nx, self.ny = nx, ny
+        self.handle = ctypes.create_string_buffer(HANDLE_BYTES)
+        if ncoef is None:
+            ncoef = H * V
+        self._alive = False
+        _check(lib().custen_create(self.handle, variant, dtype, device, num_tiles, nx, ny, block_x, block_y,
+                                   addr(out), addr(inp), addr(coef), H, L, R, V, T, B, ncoef, addr(func)))
+        self._alive = True
+
+    def compute(self, offload: int = DEVICE, stream=None) -> None:
+        if stream is None:
+            _check(lib().custen_compute(self.handle, offload))
+        else:
+            s = stream if isinstance(stream, int) else int(getattr(stream, "cuda_stream", 0))
+            _check(lib().custen_compute_on_stream(self.handle, offload, s))
+
+    def swap(self, new_input) -> None:
+        _check(lib().custen_swap(self.handle, addr(new_input)))
+
+    def set_stream(self, stream) -> None:
+        s = stream if (stream is None or isinstance(stream, int)) else int(stream.cuda_stream)
+        _check(lib().custen_set_stream(self.handle, s))
+
+    def destroy(self) -> None:
+        if self._alive:
+            self._alive = False
+            _check(lib().custen_destroy(self.handle))
+
+    def field(self, name: str):
+        """Read a cuSten_t field by name (layout of cuSten/src/struct/cuSten_struct_type.h:84-122)."""
+        return getattr(CuStenT.from_buffer(self.handle), name)
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class CuStenT(ctypes.Structure):
+    """ctypes view of cuSten_t (cuSten/src/struct/cuSten_struct_type.h:84-122)."""
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "deviceNum", "numStreams", "numTiles", "nx", "ny", "nyTile", "numSten", "numStenLeft", "numStenRight",
+        "numStenTop", "numStenBottom", "numStenHoriz", "numStenVert", "BLOCK_X", "BLOCK_Y", "xGrid", "yGrid",
+        "mem_shared")] + [
+        ("dataInput", ctypes.c_void_p), ("dataOutput", ctypes.c_void_p), ("uVel", ctypes.c_void_p),
+        ("vVel", ctypes.c_void_p), ("weights", ctypes.c_void_p), ("coe", ctypes.c_void_p),
+        ("coeDx", ctypes.c_double), ("coeDy", ctypes.c_double), ("numCoe", ctypes.c_int), ("nxLocal", ctypes.c_int),
+        ("nyLocal", ctypes.c_int), ("boundaryTop", ctypes.c_void_p), ("boundaryBottom", ctypes.c_void_p),
+        ("numBoundaryTop", ctypes.c_int), ("numBoundaryBottom", ctypes.c_int), ("streams", ctypes.c_void_p),
+        ("events", ctypes.c_void_p), ("devFunc", ctypes.c_void_p)]
+
+
+assert ctypes.sizeof(CuStenT) == HANDLE_BYTES
+
+
+def create_reference_style(variant: int, nx: int, ny: int, out, inp, coef, *, num_sten=None, L=0, R=0, T=0, B=0,
+                           H=None, V=None, num_tiles=1, block_x=32, block_y=8, num_coe=None, func=None,
+                           dtype=F64, device=0) -> Stencil:
+    """Create a handle from the reference's per-variant argument meaning (numSten / numCoe)."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    fun = variant in (XPFUN, XNPFUN, YPFUN, YNPFUN, XYPFUN, XYNPFUN)
+    if d == 0:
+        Hh, Vv = (L + R + 1 if fun else num_sten), 1
+        ncoef = num_coe if fun else num_sten
+    elif d == 1:
+        Hh, Vv = 1, (T + B + 1 if fun else num_sten)
+        ncoef = (num_coe if variant == YPFUN else num_sten) if fun else num_sten
+    else:
+        Hh, Vv = H, V
+        ncoef = H * V
+    return Stencil(variant, nx, ny, out, inp, coef, H=Hh, L=L, R=R, V=Vv, T=T, B=B, num_tiles=num_tiles,
+                   block_x=block_x, block_y=block_y, dtype=dtype, device=device, ncoef=ncoef, func=func)

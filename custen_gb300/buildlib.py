@@ -1,0 +1,98 @@
+"""Build recipe for the sm_103a libraries of this package.
+
+Outputs (in-tree, git-ignored):
+  custen_gb300/libcusten_gb300.so  -- shared library: C-ABI (include/custen_gb300.h), the C++ drop-in API
+                                      (include/cuSten.h), kernels and the shipped Fun device functions.
+  custen_gb300/libcuSten.a         -- static drop-in for the reference's libcuSten.a (relocatable device
+                                      code; link the user program with nvcc -rdc=true, as with the reference).
+
+Every translation unit is compiled for sm_103a only, with relocatable device code so that the Fun
+variants can call device functions defined in other translation units.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = ROOT / "_build" / "custen_gb300"
+SO_PATH = PKG / "libcusten_gb300.so"
+A_PATH = PKG / "libcuSten.a"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
+
+# Translation units of the static drop-in library (the reference's libcuSten.a surface).
+LIB_SOURCES = ["plan.cu", "stencil_f64.cu", "stencil_f32.cu"]
+# Extra translation units of the shared library.
+SO_SOURCES = ["builtin_funs.cu"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"command failed ({proc.returncode}): {' '.join(cmd)}\n{proc.stdout}")
+
+
+def _needs(out: Path, deps: list[Path]) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def _headers() -> list[Path]:
+    return sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
+
+
+def build(verbose: bool = False, jobs: int | None = None) -> Path:
+    BUILD.mkdir(parents=True, exist_ok=True)
+    cc = nvcc()
+    hdrs = _headers()
+    srcs = LIB_SOURCES + SO_SOURCES
+    objs = {s: BUILD / (Path(s).stem + ".o") for s in srcs}
+
+    def compile_one(src: str) -> None:
+        out = objs[src]
+        if _needs(out, [CSRC / src] + hdrs):
+            cmd = [cc, *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(out)]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            _run(cmd)
+
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
+        list(ex.map(compile_one, srcs))
+
+    all_objs = [str(objs[s]) for s in srcs]
+    if _needs(SO_PATH, [objs[s] for s in srcs]):
+        tmp = SO_PATH.with_suffix(".so.tmp")
+        _run([cc, *ARCH, "-shared", "-rdc=true", "-Xcompiler", "-fPIC", *all_objs, "-o", str(tmp), "-cudart",
+              "static"])
+        os.replace(tmp, SO_PATH)
+    lib_objs = [objs[s] for s in LIB_SOURCES]
+    if _needs(A_PATH, lib_objs):
+        tmp = A_PATH.with_suffix(".a.tmp")
+        if tmp.exists():
+            tmp.unlink()
+        _run([cc, *ARCH, "--lib", *[str(o) for o in lib_objs], "-o", str(tmp)])
+        os.replace(tmp, A_PATH)
+    return SO_PATH
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print(SO_PATH)

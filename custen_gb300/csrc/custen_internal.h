@@ -1,0 +1,133 @@
+// Internal definitions shared by the host plan layer and the stencil kernels.
+//
+// Variant numbering, window geometry and the per-point write rules below restate the behaviour of
+// the reference kernels (cuSten/src/kernels/2d_{x,y,xy}_{p,np}[_fun]_kernel.cu); each rule cites
+// the reference lines it follows.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace custen {
+
+enum Variant : int {
+    V_XP = 0, V_XNP = 1, V_XPFUN = 2, V_XNPFUN = 3,
+    V_YP = 4, V_YNP = 5, V_YPFUN = 6, V_YNPFUN = 7,
+    V_XYP = 8, V_XYNP = 9, V_XYPFUN = 10, V_XYNPFUN = 11,
+    V_COUNT = 12
+};
+
+enum DType : int { DT_F64 = 0, DT_F32 = 1 };
+
+__host__ __device__ inline bool variant_is_fun(int v) { return v == V_XPFUN || v == V_XNPFUN || v == V_YPFUN || v == V_YNPFUN ||
+                                           v == V_XYPFUN || v == V_XYNPFUN; }
+__host__ __device__ inline bool variant_is_periodic(int v) { return v == V_XP || v == V_XPFUN || v == V_YP || v == V_YPFUN ||
+                                                v == V_XYP || v == V_XYPFUN; }
+__host__ __device__ inline int variant_dir(int v) { return v < 4 ? 0 : (v < 8 ? 1 : 2); }   // 0 = X, 1 = Y, 2 = XY
+
+// Per-point outcome of one Compute.
+enum Action : int { ACT_SKIP = 0, ACT_WRITE = 1, ACT_ZERO = 2 };
+
+// Arguments of one stencil launch. A launch covers `rows` consecutive rows of the field starting at
+// field row `row0` (a whole tile, or the whole field when the tiles are contiguous).
+struct StencilArgs {
+    void* out;            // output row row0
+    const void* in;       // input row row0
+    const void* top;      // T halo rows above the launch (row-major, stride nx); may be null if unused
+    const void* bot;      // B halo rows below the launch; may be null if unused
+    const void* coef;     // weights (plain variants) or coefficients (Fun variants), device-readable
+    void* func;           // device function pointer (Fun variants)
+    int nx;               // columns
+    int rows;             // rows in this launch
+    int row0;             // field row of launch row 0
+    int L, R, T, B;       // halo extents
+    int H, V;             // window width and height (weights are w[j*H+i])
+    int ncoef;            // number of weights/coefficients staged per CTA
+    int variant;          // Variant
+    int bx, by;           // the caller's BLOCK_X / BLOCK_Y (only the non-periodic write rules use them)
+    int nyTile;           // rows per tile
+    int numTiles;
+    int wrap_x;           // 1: columns outside [0,nx) wrap around (periodic variants)
+    int has_top, has_bot; // 1: halo rows above / below may be read
+    int vec_ok;           // 1: rows are 16-byte aligned, vector loads/stores allowed
+};
+
+// Write rule of the reference for point (x, gy) of the field, gy a field row.
+__host__ __device__ inline int point_action(int variant, int x, int gy, int nx, int L, int R, int T, int B,
+                                            int bx, int by, int nyTile, int numTiles) {
+    switch (variant) {
+    case V_XNP:
+        // kernel2DXnp: block 0 skips threads tx < L (2d_x_np_kernel.cu:137); the last block stores
+        // the zero-initialised sum for tx >= BLOCK_X - R (:164-176, store outside the if).
+        if (x < L) return ACT_SKIP;
+        if (x >= nx - R) return ACT_ZERO;
+        return ACT_WRITE;
+    case V_XNPFUN:
+        // kernel2DXnpFun: tx < L skipped in block 0 (2d_x_np_fun_kernel.cu:144-149), tx >= BX - R
+        // skipped in the last block (:165-170).
+        if (x < L || x >= nx - R) return ACT_SKIP;
+        return ACT_WRITE;
+    case V_YNP:
+    case V_YNPFUN: {
+        // kernel2DYnp / kernel2DYnpFun: in the first tile block row 0 stores rows T..BY-1 only
+        // (2d_y_np_kernel.cu:167-192, 2d_y_np_fun_kernel.cu:173-193); in the last tile the last block
+        // row stores ty < BY - B (2d_y_np_kernel.cu:246-249, 2d_y_np_fun_kernel.cu:242).
+        int t = gy / nyTile, yt = gy - t * nyTile;
+        if (t == 0 && yt < T) return ACT_SKIP;
+        if (t == numTiles - 1 && yt >= nyTile - B) return ACT_SKIP;
+        return ACT_WRITE;
+    }
+    case V_XYNP:
+    case V_XYNPFUN: {
+        // kernel2DXYnp: nine block cases tested in this order (2d_xy_np_kernel.cu:136-958).
+        int t = gy / nyTile, yt = gy - t * nyTile;
+        int bxi = x / bx, tx = x - bxi * bx, nbx = nx / bx;
+        int byi = yt / by, ty = yt - byi * by, nby = nyTile / by;
+        bool tileTop = (t == 0), tileBottom = (t == numTiles - 1);
+        bool left = (bxi == 0), right = (bxi == nbx - 1), topb = (byi == 0), botb = (byi == nby - 1);
+        bool ok;
+        if (left && topb) ok = tileTop ? (tx >= L && ty >= T) : (tx >= L);                      // :208-219
+        else if (right && topb) ok = tileTop ? (tx < bx - R && ty >= T) : (tx < bx - R);        // :301-312
+        else if (left && botb) ok = tileBottom ? (tx >= L && ty < by - B) : (tx >= L);          // :393-404
+        else if (right && botb) ok = tileBottom ? (tx < bx - R && ty < by - B) : (tx < bx - R); // :484-495
+        else if (topb) ok = tileTop ? (ty >= T) : true;                                         // :593-602
+        else if (botb) ok = tileBottom ? (ty < by - B) : true;                                  // :699-708
+        else if (left) ok = (tx >= L);                                                          // :784
+        // Right edge, middle block rows: the reference guard is tx < BX - L (:862; :787 for Fun).
+        // When L < R the reference stores values read from shared memory it never loaded for
+        // tx in [BX-R, BX-L); those points are left untouched here.
+        else if (right) ok = (tx < bx - L) && (tx < bx - R);
+        else ok = true;
+        return ok ? ACT_WRITE : ACT_SKIP;
+    }
+    default:
+        return ACT_WRITE;   // periodic variants write every point
+    }
+}
+
+// Private per-handle state. It lives in the same allocation as the handle's stream array (the
+// reference allocates `streams` with malloc and only Destroy frees it), so cuSten_t keeps its layout.
+struct PlanPrivate {
+    uint32_t magic;
+    int variant;
+    int dtype;
+    int H, V, L, R, T, B;
+    int ncoef;            // weights or coefficients read per Compute
+    int mem_kind;         // -1 unknown, 0 device, 1 managed, 2 host-accessible system memory
+    cudaStream_t user_stream;
+    int use_user_stream;
+    unsigned long long launches;   // kernels launched by this handle (for instrumentation)
+};
+
+struct StreamBlock {
+    cudaStream_t streams[3];
+    PlanPrivate priv;
+};
+
+constexpr uint32_t kPlanMagic = 0xC5E7B300u;
+
+// Launch entry points implemented in the kernel translation units.
+cudaError_t launch_stencil_f64(const StencilArgs& a, cudaStream_t s);
+cudaError_t launch_stencil_f32(const StencilArgs& a, cudaStream_t s);
+
+}  // namespace custen

@@ -1,0 +1,648 @@
+// Host plan layer: Create / Swap / Destroy / Compute for the twelve cuSten variants, the reference's
+// C++ API (exit-on-error, cuSten/src/util/error.cu:43-53) and the status-returning C-ABI.
+//
+// The handle is filled as the reference's Create functions fill it (sizes, per-tile input/output
+// pointers, per-tile halo pointers, grid, three streams and two events): see
+// cuSten/src/struct/custenCreateDestroy2D*.cu. Compute differs in how it runs, not in what it
+// computes: when the tiles are contiguous in memory and the data is device-resident, the whole field
+// is one launch (the per-tile halo pointers then name rows of the same array); otherwise one launch
+// per tile reads its halo rows through the handle's boundaryTop/boundaryBottom pointers.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "../../include/cuSten.h"
+#include "../../include/custen_gb300.h"
+#include "custen_internal.h"
+
+static_assert(sizeof(cuSten_t) == 200, "cuSten_t must keep the reference layout (200 bytes)");
+static_assert(offsetof(cuSten_t, weights) == 104, "cuSten_t::weights offset");
+static_assert(offsetof(cuSten_t, streams) == 176, "cuSten_t::streams offset");
+static_assert(offsetof(cuSten_t, devFunc) == 192, "cuSten_t::devFunc offset");
+
+namespace custen {
+
+static thread_local std::string g_last_error;
+static std::atomic<unsigned long long> g_launches{0};
+
+enum { ST_OK = 0, ST_CUDA = 1, ST_ARG = 2, ST_UNSUPPORTED = 3 };
+
+static int fail_cuda(cudaError_t e, const char* action) {
+    char buf[1024];
+    snprintf(buf, sizeof(buf), "Error while '%s': %s", action, cudaGetErrorString(e));
+    g_last_error = buf;
+    cudaGetLastError();   // clear the sticky-free error so the next call starts clean
+    return ST_CUDA;
+}
+
+static int fail_arg(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return ST_ARG;
+}
+
+#define CU_TRY(expr, action)                          \
+    do {                                              \
+        cudaError_t _e = (expr);                      \
+        if (_e != cudaSuccess) return fail_cuda(_e, action); \
+    } while (0)
+
+static PlanPrivate* priv_of(const cuSten_t* h) {
+    if (h == nullptr || h->streams == nullptr) return nullptr;
+    StreamBlock* blk = reinterpret_cast<StreamBlock*>(h->streams);
+    if (blk->priv.magic != kPlanMagic) return nullptr;
+    return &blk->priv;
+}
+
+static inline char* byte_ptr(void* p) { return reinterpret_cast<char*>(p); }
+
+// Periodic halo pointers from `in` (the formulas of every Y/XY Create and Swap, e.g.
+// custenCreateDestroy2DYp.cu:182-216 and :248-282).
+static void set_halos_periodic(cuSten_t* h, void* in, int esz) {
+    const size_t nx = h->nx;
+    const int nt = h->numTiles, ny = h->ny, nyT = h->nyTile, T = h->numStenTop;
+    char* base = byte_ptr(in);
+    for (int t = 0; t < nt; ++t) {
+        long top_row = (t == 0) ? (long)(ny - T) : (long)t * nyT - T;
+        long bot_row = (t == nt - 1) ? 0 : (long)(t + 1) * nyT;
+        h->boundaryTop[t] = reinterpret_cast<double*>(base + top_row * (long)nx * esz);
+        h->boundaryBottom[t] = reinterpret_cast<double*>(base + bot_row * (long)nx * esz);
+    }
+}
+
+// Edge-clamped halo pointers of cuStenCreate2DYnp (custenCreateDestroy2DYnp.cu:182-216): the first
+// tile's top and the last tile's bottom name rows of the field itself (they are never read).
+static void set_halos_ynp_create(cuSten_t* h, void* in, int esz) {
+    const size_t nx = h->nx;
+    const int nt = h->numTiles, ny = h->ny, nyT = h->nyTile, T = h->numStenTop, B = h->numStenBottom;
+    char* base = byte_ptr(in);
+    for (int t = 0; t < nt; ++t) {
+        long top_row = (t == 0) ? 0 : (long)t * nyT - T;
+        long bot_row = (t == nt - 1) ? (long)(ny - B) : (long)(t + 1) * nyT;
+        h->boundaryTop[t] = reinterpret_cast<double*>(base + top_row * (long)nx * esz);
+        h->boundaryBottom[t] = reinterpret_cast<double*>(base + bot_row * (long)nx * esz);
+    }
+}
+
+static int destroy_plan(cuSten_t* h);
+
+int create_plan(cuSten_t* h, int variant, int dtype, int dev, int numTiles, int nx, int ny, int BX, int BY,
+                void* out, void* in, void* coef, int H, int L, int R, int V, int T, int B, int ncoef, void* func,
+                int numStenField) {
+    if (h == nullptr) return fail_arg("cuSten handle is NULL");
+    if (variant < 0 || variant >= V_COUNT) return fail_arg("unknown stencil variant %d", variant);
+    if (dtype != DT_F64 && dtype != DT_F32) return fail_arg("unknown data type %d", dtype);
+    if (numTiles < 1) return fail_arg("numTiles must be >= 1 (got %d)", numTiles);
+    if (nx < 1 || ny < 1) return fail_arg("nx and ny must be >= 1 (got %d x %d)", nx, ny);
+    if (ny % numTiles != 0) return fail_arg("ny (%d) must be divisible by numTiles (%d)", ny, numTiles);
+    if (BX < 1 || BY < 1) return fail_arg("BLOCK_X and BLOCK_Y must be >= 1");
+    if (L < 0 || R < 0 || T < 0 || B < 0) return fail_arg("stencil extents must be >= 0");
+    if (H < 1 || V < 1) return fail_arg("stencil size must be >= 1");
+    if (H > L + R + 1 || V > T + B + 1)
+        return fail_arg("stencil (%d x %d) reaches beyond its halo (L=%d R=%d T=%d B=%d)", H, V, L, R, T, B);
+    const int nyTile = ny / numTiles;
+    if (L >= nx || R >= nx || T > nyTile || B > nyTile)
+        return fail_arg("halo larger than the field or tile (nx=%d nyTile=%d L=%d R=%d T=%d B=%d)", nx, nyTile, L,
+                        R, T, B);
+    const bool np = !variant_is_periodic(variant);
+    if (np && (nx % BX != 0 || nyTile % BY != 0))
+        return fail_arg("non-periodic stencils need nx %% BLOCK_X == 0 and nyTile %% BLOCK_Y == 0 "
+                        "(nx=%d nyTile=%d BLOCK_X=%d BLOCK_Y=%d)", nx, nyTile, BX, BY);
+    if (ncoef < 0 || ncoef > 4096) return fail_arg("number of weights/coefficients out of range (%d)", ncoef);
+    if (ncoef > 0 && coef == nullptr) return fail_arg("weights/coefficients pointer is NULL");
+    if (variant_is_fun(variant) && func == nullptr) return fail_arg("device function pointer is NULL");
+    if (in == nullptr || out == nullptr) return fail_arg("data pointers must not be NULL");
+
+    CU_TRY(cudaSetDevice(dev), "Setting current device");
+
+    StreamBlock* blk = static_cast<StreamBlock*>(calloc(1, sizeof(StreamBlock)));
+    if (!blk) return fail_arg("out of host memory");
+    for (int s = 0; s < 3; ++s) {
+        cudaError_t e = cudaStreamCreate(&blk->streams[s]);
+        if (e != cudaSuccess) {
+            for (int k = 0; k < s; ++k) cudaStreamDestroy(blk->streams[k]);
+            free(blk);
+            return fail_cuda(e, "Creating stream");
+        }
+    }
+    cudaEvent_t* events = static_cast<cudaEvent_t*>(malloc(2 * sizeof(cudaEvent_t)));
+    for (int ev = 0; ev < 2; ++ev) {
+        cudaError_t e = cudaEventCreateWithFlags(&events[ev], cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            for (int k = 0; k < ev; ++k) cudaEventDestroy(events[k]);
+            for (int k = 0; k < 3; ++k) cudaStreamDestroy(blk->streams[k]);
+            free(events);
+            free(blk);
+            return fail_cuda(e, "Creating event");
+        }
+    }
+    PlanPrivate& p = blk->priv;
+    p.magic = kPlanMagic;
+    p.variant = variant;
+    p.dtype = dtype;
+    p.H = H; p.V = V; p.L = L; p.R = R; p.T = T; p.B = B;
+    p.ncoef = ncoef;
+    p.mem_kind = -1;
+    p.user_stream = nullptr;
+    p.use_user_stream = 0;
+    p.launches = 0;
+
+    const int esz = dtype == DT_F64 ? 8 : 4;
+    const int dir = variant_dir(variant);
+    memset(h, 0, sizeof(*h));
+    h->deviceNum = dev;
+    h->numStreams = 3;
+    h->numTiles = numTiles;
+    h->nx = nx;
+    h->ny = ny;
+    h->nyTile = nyTile;
+    h->numSten = numStenField;
+    h->numStenLeft = L;
+    h->numStenRight = R;
+    h->numStenTop = T;
+    h->numStenBottom = B;
+    h->numStenHoriz = (dir == 2) ? H : 0;
+    h->numStenVert = (dir == 2) ? V : 0;
+    h->BLOCK_X = BX;
+    h->BLOCK_Y = BY;
+    h->xGrid = (nx % BX == 0) ? nx / BX : nx / BX + 1;
+    h->yGrid = (nyTile % BY == 0) ? nyTile / BY : nyTile / BY + 1;
+    h->nxLocal = BX + L + R;
+    h->nyLocal = BY + T + B;
+    h->mem_shared = (int)(((size_t)h->nxLocal * h->nyLocal + (size_t)ncoef) * sizeof(double));
+    if (variant_is_fun(variant)) {
+        h->coe = static_cast<double*>(coef);
+        h->numCoe = ncoef;
+        h->devFunc = static_cast<double*>(func);
+    } else {
+        h->weights = static_cast<double*>(coef);
+    }
+    h->streams = blk->streams;
+    h->events = events;
+    h->dataInput = static_cast<double**>(malloc(numTiles * sizeof(double*)));
+    h->dataOutput = static_cast<double**>(malloc(numTiles * sizeof(double*)));
+    const size_t tile_bytes = (size_t)nx * nyTile * esz;
+    for (int t = 0; t < numTiles; ++t) {
+        h->dataInput[t] = reinterpret_cast<double*>(byte_ptr(in) + t * tile_bytes);
+        h->dataOutput[t] = reinterpret_cast<double*>(byte_ptr(out) + t * tile_bytes);
+    }
+    if (dir != 0) {
+        h->boundaryTop = static_cast<double**>(malloc(numTiles * sizeof(double*)));
+        h->boundaryBottom = static_cast<double**>(malloc(numTiles * sizeof(double*)));
+        if (variant == V_YNP || variant == V_YNPFUN) set_halos_ynp_create(h, in, esz);
+        else set_halos_periodic(h, in, esz);
+        h->numBoundaryTop = T * nx;
+        h->numBoundaryBottom = B * nx;
+    }
+    return ST_OK;
+}
+
+static int destroy_plan(cuSten_t* h) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    cudaSetDevice(h->deviceNum);
+    StreamBlock* blk = reinterpret_cast<StreamBlock*>(h->streams);
+    int st = ST_OK;
+    for (int s = 0; s < 3; ++s) {
+        cudaError_t e = cudaStreamDestroy(blk->streams[s]);
+        if (e != cudaSuccess && st == ST_OK) st = fail_cuda(e, "Destroying stream");
+    }
+    for (int ev = 0; ev < 2; ++ev) {
+        cudaError_t e = cudaEventDestroy(h->events[ev]);
+        if (e != cudaSuccess && st == ST_OK) st = fail_cuda(e, "Destroying event");
+    }
+    blk->priv.magic = 0;
+    free(blk);
+    free(h->events);
+    free(h->dataInput);
+    free(h->dataOutput);
+    free(h->boundaryTop);
+    free(h->boundaryBottom);
+    h->streams = nullptr;
+    h->events = nullptr;
+    h->dataInput = h->dataOutput = h->boundaryTop = h->boundaryBottom = nullptr;
+    return st;
+}
+
+static int swap_plan(cuSten_t* h, void* newInput) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    for (int t = 0; t < h->numTiles; ++t) {
+        double* tmp = h->dataInput[t];
+        h->dataInput[t] = h->dataOutput[t];
+        h->dataOutput[t] = tmp;
+    }
+    // X variants ignore the argument (custenCreateDestroy2DXp.cu:179-190); Y and XY variants
+    // recompute every halo pointer from it with the periodic formulas, Ynp included
+    // (custenCreateDestroy2DYnp.cu:248-282).
+    if (variant_dir(p->variant) != 0) {
+        if (newInput == nullptr) return fail_arg("Swap needs the new input pointer for Y/XY stencils");
+        set_halos_periodic(h, newInput, p->dtype == DT_F64 ? 8 : 4);
+    }
+    return ST_OK;
+}
+
+static int memory_kind(const void* ptr) {
+    cudaPointerAttributes at;
+    cudaError_t e = cudaPointerGetAttributes(&at, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 2;
+    }
+    switch (at.type) {
+    case cudaMemoryTypeManaged: return 1;
+    case cudaMemoryTypeDevice: return 0;
+    default: return 2;   // pinned or system memory: read in place (NVLink-C2C on Grace systems)
+    }
+}
+
+static cudaError_t prefetch(const void* p, size_t bytes, int dev, cudaStream_t s) {
+    if (p == nullptr || bytes == 0) return cudaSuccess;
+    cudaMemLocation loc;
+    if (dev >= 0) {
+        loc.type = cudaMemLocationTypeDevice;
+        loc.id = dev;
+    } else {
+        loc.type = cudaMemLocationTypeHost;
+        loc.id = 0;
+    }
+    return cudaMemPrefetchAsync(p, bytes, loc, 0, s);
+}
+
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+static cudaError_t launch(const StencilArgs& a, int dtype, cudaStream_t s, PlanPrivate* p) {
+    cudaError_t e = dtype == DT_F64 ? launch_stencil_f64(a, s) : launch_stencil_f32(a, s);
+    if (e == cudaSuccess) {
+        ++p->launches;
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    }
+    return e;
+}
+
+int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    CU_TRY(cudaSetDevice(h->deviceNum), "Setting current device");
+    cudaStream_t s = explicit_stream ? *explicit_stream : (p->use_user_stream ? p->user_stream : h->streams[0]);
+    cudaStream_t copy_s = explicit_stream ? *explicit_stream : (p->use_user_stream ? p->user_stream : h->streams[1]);
+    const int esz = p->dtype == DT_F64 ? 8 : 4;
+    const int nt = h->numTiles, nx = h->nx, nyT = h->nyTile;
+    const int dir = variant_dir(p->variant);
+    const bool periodic = variant_is_periodic(p->variant);
+    const size_t tile_bytes = (size_t)nx * nyT * esz;
+
+    StencilArgs a;
+    memset(&a, 0, sizeof(a));
+    a.coef = variant_is_fun(p->variant) ? (const void*)h->coe : (const void*)h->weights;
+    a.func = variant_is_fun(p->variant) ? (void*)h->devFunc : nullptr;
+    a.nx = nx;
+    a.L = p->L; a.R = p->R; a.T = p->T; a.B = p->B;
+    a.H = p->H; a.V = p->V;
+    a.ncoef = p->ncoef;
+    a.variant = p->variant;
+    a.bx = h->BLOCK_X;
+    a.by = h->BLOCK_Y;
+    a.nyTile = nyT;
+    a.numTiles = nt;
+    a.wrap_x = periodic && dir != 1;
+
+    // Tiles contiguous and every interior halo pointer naming the neighbouring rows of that array?
+    char* in0 = byte_ptr(h->dataInput[0]);
+    char* out0 = byte_ptr(h->dataOutput[0]);
+    bool contiguous = true;
+    for (int t = 0; t < nt && contiguous; ++t) {
+        if (byte_ptr(h->dataInput[t]) != in0 + t * tile_bytes) contiguous = false;
+        if (byte_ptr(h->dataOutput[t]) != out0 + t * tile_bytes) contiguous = false;
+        if (dir != 0 && contiguous) {
+            if (t > 0 && p->T > 0 &&
+                byte_ptr(h->boundaryTop[t]) != in0 + ((long)t * nyT - p->T) * (long)nx * esz)
+                contiguous = false;
+            if (t < nt - 1 && p->B > 0 && byte_ptr(h->boundaryBottom[t]) != in0 + (long)(t + 1) * nyT * nx * esz)
+                contiguous = false;
+        }
+    }
+
+    const int kind = memory_kind(in0);
+    p->mem_kind = kind;
+    const bool row_aligned = ((size_t)nx * esz) % 16 == 0;
+
+    auto fill_launch = [&](int t_first, int t_count) {
+        a.in = h->dataInput[t_first];
+        a.out = h->dataOutput[t_first];
+        a.rows = t_count * nyT;
+        a.row0 = t_first * nyT;
+        const int t_last = t_first + t_count - 1;
+        a.top = (dir != 0) ? (const void*)h->boundaryTop[t_first] : nullptr;
+        a.bot = (dir != 0) ? (const void*)h->boundaryBottom[t_last] : nullptr;
+        a.has_top = (dir != 0 && p->T > 0) && (periodic || t_first > 0);
+        a.has_bot = (dir != 0 && p->B > 0) && (periodic || t_last < nt - 1);
+        a.vec_ok = row_aligned && aligned16(a.in) && aligned16(a.out) && (!a.has_top || aligned16(a.top)) &&
+                   (!a.has_bot || aligned16(a.bot));
+    };
+
+    if (kind != 1) {
+        // Device-resident (or directly addressable) data: no migration needed.
+        if (contiguous) {
+            fill_launch(0, nt);
+            CU_TRY(launch(a, p->dtype, s, p), "Computing stencil");
+        } else {
+            for (int t = 0; t < nt; ++t) {
+                fill_launch(t, 1);
+                CU_TRY(launch(a, p->dtype, s, p), "Computing stencil tile");
+            }
+        }
+        return ST_OK;
+    }
+
+    // Managed memory: stream the tiles through the GPU as the reference does
+    // (cuSten/src/kernels/2d_x_p_kernel.cu:216-271): prefetch tile t+1 (and its halo rows) on the copy
+    // stream while tile t computes; with HOST offload send each finished tile back to the host.
+    // The ordering is expressed with events, so the host never blocks.
+    const int dev = h->deviceNum;
+    const size_t halo_top_bytes = (size_t)p->T * nx * esz, halo_bot_bytes = (size_t)p->B * nx * esz;
+    CU_TRY(prefetch(a.coef, (size_t)p->ncoef * esz, dev, copy_s), "Prefetching weights");
+    auto prefetch_tile = [&](int t) -> cudaError_t {
+        cudaError_t e = prefetch(h->dataInput[t], tile_bytes, dev, copy_s);
+        if (e == cudaSuccess) e = prefetch(h->dataOutput[t], tile_bytes, dev, copy_s);
+        if (e == cudaSuccess && dir != 0 && halo_top_bytes) e = prefetch(h->boundaryTop[t], halo_top_bytes, dev, copy_s);
+        if (e == cudaSuccess && dir != 0 && halo_bot_bytes) e = prefetch(h->boundaryBottom[t], halo_bot_bytes, dev, copy_s);
+        if (e == cudaSuccess) e = cudaEventRecord(h->events[t & 1], copy_s);
+        return e;
+    };
+    CU_TRY(prefetch_tile(0), "Prefetching tile");
+    for (int t = 0; t < nt; ++t) {
+        CU_TRY(cudaStreamWaitEvent(s, h->events[t & 1], 0), "Ordering tile after prefetch");
+        fill_launch(t, 1);
+        CU_TRY(launch(a, p->dtype, s, p), "Computing stencil tile");
+        if (offload == HOST) {
+            CU_TRY(prefetch(h->dataOutput[t], tile_bytes, -1, s), "Offloading output tile");
+            CU_TRY(prefetch(h->dataInput[t], tile_bytes, -1, s), "Offloading input tile");
+        }
+        if (t + 1 < nt) CU_TRY(prefetch_tile(t + 1), "Prefetching tile");
+    }
+    if (copy_s != s) {
+        // Later work on the compute stream must also follow the last prefetch.
+        CU_TRY(cudaEventRecord(h->events[0], copy_s), "Recording event");
+        CU_TRY(cudaStreamWaitEvent(s, h->events[0], 0), "Ordering compute after copies");
+    }
+    return ST_OK;
+}
+
+}  // namespace custen
+
+using namespace custen;
+
+// ---------------------------------------------------------------------------------------------
+// Reference C++ API (exit on error, as cuSten/src/util/error.cu:43-53 does)
+// ---------------------------------------------------------------------------------------------
+
+void checkError(const char* action) {
+    cudaError_t error = cudaGetLastError();
+    if (error != cudaSuccess) {
+        printf("\nError while '%s': %s\nprogram terminated ...\n\n", action, cudaGetErrorString(error));
+        exit(EXIT_FAILURE);
+    }
+}
+
+static void exit_on(int st) {
+    if (st != ST_OK) {
+        printf("\n%s\nprogram terminated ...\n\n", g_last_error.c_str());
+        exit(EXIT_FAILURE);
+    }
+}
+
+// ---- X ----
+void cuStenCreate2DXp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                      double* w, int numSten, int L, int R) {
+    exit_on(create_plan(h, V_XP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, numSten, L, R, 1, 0, 0, numSten,
+                        nullptr, numSten));
+}
+void cuStenCreate2DXnp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                       double* w, int numSten, int L, int R) {
+    exit_on(create_plan(h, V_XNP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, numSten, L, R, 1, 0, 0, numSten,
+                        nullptr, numSten));
+}
+void cuStenCreate2DXpFun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                         double* coe, int numSten, int L, int R, int numCoe, double* func) {
+    exit_on(create_plan(h, V_XPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, L + R + 1, L, R, 1, 0, 0,
+                        numCoe, func, numSten));
+}
+void cuStenCreate2DXnpFun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                          double* coe, int numSten, int L, int R, int numCoe, double* func) {
+    exit_on(create_plan(h, V_XNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, L + R + 1, L, R, 1, 0, 0,
+                        numCoe, func, numSten));
+}
+// ---- Y ----
+void cuStenCreate2DYp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                      double* w, int numSten, int T, int B) {
+    exit_on(create_plan(h, V_YP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, 1, 0, 0, numSten, T, B, numSten,
+                        nullptr, numSten));
+}
+void cuStenCreate2DYnp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                       double* w, int numSten, int T, int B) {
+    exit_on(create_plan(h, V_YNP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, 1, 0, 0, numSten, T, B, numSten,
+                        nullptr, numSten));
+}
+void cuStenCreate2DYpFun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                         double* coe, int numSten, int T, int B, int numCoe, double* func) {
+    exit_on(create_plan(h, V_YPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, 1, 0, 0, T + B + 1, T, B,
+                        numCoe, func, numSten));
+}
+void cuStenCreate2DYnpFun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                          double* coe, int numSten, int T, int B, double* func) {
+    // kernel2DYnpFun copies numSten coefficients (2d_y_np_fun_kernel.cu:102).
+    exit_on(create_plan(h, V_YNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, 1, 0, 0, T + B + 1, T, B,
+                        numSten, func, numSten));
+}
+// ---- XY ----
+void cuStenCreate2DXYp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                       double* w, int Hs, int L, int R, int Vs, int T, int B) {
+    exit_on(create_plan(h, V_XYP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, Hs, L, R, Vs, T, B, Hs * Vs,
+                        nullptr, Hs * Vs));
+}
+void cuStenCreate2DXYnp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                        double* w, int Hs, int L, int R, int Vs, int T, int B) {
+    exit_on(create_plan(h, V_XYNP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, Hs, L, R, Vs, T, B, Hs * Vs,
+                        nullptr, Hs * Vs));
+}
+void cuStenCreate2DXYpFun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                          double* coe, int Hs, int L, int R, int Vs, int T, int B, double* func) {
+    // kernel2DXYpFun copies numSten = H*V coefficients (2d_xy_p_fun_kernel.cu:114-118).
+    exit_on(create_plan(h, V_XYPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, Hs, L, R, Vs, T, B, Hs * Vs,
+                        func, Hs * Vs));
+}
+void cuStenCreate2DXYnpFun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                           double* coe, int Hs, int L, int R, int Vs, int T, int B, double* func) {
+    exit_on(create_plan(h, V_XYNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, Hs, L, R, Vs, T, B, Hs * Vs,
+                        func, Hs * Vs));
+}
+
+#define CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(SUFFIX)                                                  \
+    void cuStenSwap2D##SUFFIX(cuSten_t* h, double* dataInput) { exit_on(swap_plan(h, dataInput)); }  \
+    void cuStenDestroy2D##SUFFIX(cuSten_t* h) { exit_on(destroy_plan(h)); }                          \
+    void cuStenCompute2D##SUFFIX(cuSten_t* h, bool offload) { exit_on(compute_plan(h, offload ? 1 : 0, nullptr)); }
+
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(Xp)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(Xnp)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XpFun)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XnpFun)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(Yp)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(Ynp)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(YpFun)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(YnpFun)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYp)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYnp)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYpFun)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYnpFun)
+
+// The reference library defines the XpFun compute under this misspelt name (2d_x_p_fun_kernel.cu:172).
+void cuSenCompute2DXpFun(cuSten_t* h, bool offload) { exit_on(compute_plan(h, offload ? 1 : 0, nullptr)); }
+
+// ---------------------------------------------------------------------------------------------
+// C-ABI
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+int custen_abi_version(void) { return 1; }
+int custen_sizeof_handle(void) { return (int)sizeof(cuSten_t); }
+const char* custen_last_error(void) { return g_last_error.c_str(); }
+unsigned long long custen_kernel_launches(void) { return g_launches.load(); }
+
+int custen_create(cuSten_t* h, int variant, int dtype, int dev, int nt, int nx, int ny, int bx, int by, void* out,
+                  void* in, void* coef, int H, int L, int R, int V, int T, int B, int ncoef, void* func) {
+    const int dir = (variant >= 0 && variant < V_COUNT) ? variant_dir(variant) : 0;
+    const int field = dir == 2 ? H * V : (dir == 0 ? H : V);
+    return create_plan(h, variant, dtype, dev, nt, nx, ny, bx, by, out, in, coef, H, L, R, V, T, B, ncoef, func,
+                       field);
+}
+int custen_compute(cuSten_t* h, int offload) { return compute_plan(h, offload, nullptr); }
+int custen_compute_on_stream(cuSten_t* h, int offload, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    return compute_plan(h, offload, &s);
+}
+int custen_swap(cuSten_t* h, void* in) { return swap_plan(h, in); }
+int custen_destroy(cuSten_t* h) { return destroy_plan(h); }
+int custen_set_stream(cuSten_t* h, void* stream) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    p->user_stream = static_cast<cudaStream_t>(stream);
+    p->use_user_stream = stream != nullptr;
+    return ST_OK;
+}
+int custen_handle_variant(const cuSten_t* h, int* variant, int* dtype) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    if (variant) *variant = p->variant;
+    if (dtype) *dtype = p->dtype;
+    return ST_OK;
+}
+
+int custen_create_2d_xp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                        double* w, int numSten, int L, int R) {
+    return create_plan(h, V_XP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, numSten, L, R, 1, 0, 0, numSten,
+                       nullptr, numSten);
+}
+int custen_create_2d_xnp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                         double* w, int numSten, int L, int R) {
+    return create_plan(h, V_XNP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, numSten, L, R, 1, 0, 0, numSten,
+                       nullptr, numSten);
+}
+int custen_create_2d_xp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out,
+                            double* in, double* coe, int numSten, int L, int R, int numCoe, double* func) {
+    return create_plan(h, V_XPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, L + R + 1, L, R, 1, 0, 0,
+                       numCoe, func, numSten);
+}
+int custen_create_2d_xnp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out,
+                             double* in, double* coe, int numSten, int L, int R, int numCoe, double* func) {
+    return create_plan(h, V_XNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, L + R + 1, L, R, 1, 0, 0,
+                       numCoe, func, numSten);
+}
+int custen_create_2d_yp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                        double* w, int numSten, int T, int B) {
+    return create_plan(h, V_YP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, 1, 0, 0, numSten, T, B, numSten,
+                       nullptr, numSten);
+}
+int custen_create_2d_ynp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                         double* w, int numSten, int T, int B) {
+    return create_plan(h, V_YNP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, 1, 0, 0, numSten, T, B, numSten,
+                       nullptr, numSten);
+}
+int custen_create_2d_yp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out,
+                            double* in, double* coe, int numSten, int T, int B, int numCoe, double* func) {
+    return create_plan(h, V_YPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, 1, 0, 0, T + B + 1, T, B,
+                       numCoe, func, numSten);
+}
+int custen_create_2d_ynp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out,
+                             double* in, double* coe, int numSten, int T, int B, double* func) {
+    return create_plan(h, V_YNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, 1, 0, 0, T + B + 1, T, B,
+                       numSten, func, numSten);
+}
+int custen_create_2d_xyp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                         double* w, int Hs, int L, int R, int Vs, int T, int B) {
+    return create_plan(h, V_XYP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, Hs, L, R, Vs, T, B, Hs * Vs,
+                       nullptr, Hs * Vs);
+}
+int custen_create_2d_xynp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out, double* in,
+                          double* w, int Hs, int L, int R, int Vs, int T, int B) {
+    return create_plan(h, V_XYNP, DT_F64, dev, nt, nx, ny, bx, by, out, in, w, Hs, L, R, Vs, T, B, Hs * Vs,
+                       nullptr, Hs * Vs);
+}
+int custen_create_2d_xyp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out,
+                             double* in, double* coe, int Hs, int L, int R, int Vs, int T, int B, double* func) {
+    return create_plan(h, V_XYPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, Hs, L, R, Vs, T, B, Hs * Vs,
+                       func, Hs * Vs);
+}
+int custen_create_2d_xynp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double* out,
+                              double* in, double* coe, int Hs, int L, int R, int Vs, int T, int B, double* func) {
+    return create_plan(h, V_XYNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, Hs, L, R, Vs, T, B, Hs * Vs,
+                       func, Hs * Vs);
+}
+
+int custen_malloc_managed(void** ptr, size_t bytes) {
+    CU_TRY(cudaMallocManaged(ptr, bytes), "Allocating managed memory");
+    return ST_OK;
+}
+int custen_malloc_device(void** ptr, size_t bytes) {
+    CU_TRY(cudaMalloc(ptr, bytes), "Allocating device memory");
+    return ST_OK;
+}
+int custen_malloc_host(void** ptr, size_t bytes) {
+    CU_TRY(cudaMallocHost(ptr, bytes), "Allocating pinned host memory");
+    return ST_OK;
+}
+int custen_free(void* ptr) {
+    CU_TRY(cudaFree(ptr), "Freeing memory");
+    return ST_OK;
+}
+int custen_free_host(void* ptr) {
+    CU_TRY(cudaFreeHost(ptr), "Freeing pinned host memory");
+    return ST_OK;
+}
+int custen_memcpy(void* dst, const void* src, size_t bytes) {
+    CU_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault), "Copying memory");
+    return ST_OK;
+}
+int custen_memset(void* ptr, int value, size_t bytes) {
+    CU_TRY(cudaMemset(ptr, value, bytes), "Setting memory");
+    return ST_OK;
+}
+int custen_device_synchronize(void) {
+    CU_TRY(cudaDeviceSynchronize(), "Synchronising device");
+    return ST_OK;
+}
+int custen_set_device(int device) {
+    CU_TRY(cudaSetDevice(device), "Setting current device");
+    return ST_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,11 @@
+// FP32 instantiation of the stencil kernels.
+#include "stencil_launch.cuh"
+
+namespace custen {
+
+cudaError_t launch_stencil_f32(const StencilArgs& a, cudaStream_t s) {
+    // 128 x 32 output tile, 4 columns x 4 rows per thread: 256 threads.
+    return launch_ldg<float, 128, 32, 4>(a, s);
+}
+
+}  // namespace custen

@@ -1,0 +1,208 @@
+// Shared-memory tiled 2D stencil kernel for sm_103a (FP64 and FP32), covering all twelve cuSten
+// variants (X / Y / XY, periodic / non-periodic, weights / device-function-pointer).
+//
+// Per point the value is the reference's FMA chain: sum = 0; for j in 0..V-1, for i in 0..H-1:
+// sum = fma(w[j*H+i], in[y-T+j][x-L+i], sum) (cuSten/src/kernels/2d_xy_p_kernel.cu:507-520; the X
+// and Y kernels are the V=1 and H=1 cases, 2d_x_p_kernel.cu:166-172, 2d_y_p_kernel.cu:120-124).
+// Exact-zero weights are dropped from the chain: fma(0, a, s) == s for every finite a and the chain
+// starts from +0.0, so the result is bit-identical for finite inputs.
+//
+// Each CTA owns an output tile of TW x TH points. It stages the (TH+T+B) x (LP+TW+RP) input window
+// in shared memory -- the rows from the launch's own rows or from the top/bottom halo pointers, the
+// columns wrapped (periodic) or zero-filled (non-periodic) -- then every thread produces VEC adjacent
+// columns x RPT rows with 16-byte vector stores. Halo tiles are staged by TMA (stencil_tma.cuh) when
+// the geometry allows; this file holds the compute/store stage and the plain-load staging path.
+#pragma once
+
+#include "custen_internal.h"
+
+namespace custen {
+
+template <typename T> struct VecT;
+template <> struct VecT<double> { using type = double2; static constexpr int n = 2; };
+template <> struct VecT<float> { using type = float4; static constexpr int n = 4; };
+
+__host__ __device__ constexpr int round_up_int(int v, int m) { return (v + m - 1) / m * m; }
+
+// Geometry of the staged window, identical on host (shared-memory sizing) and device.
+template <typename T, int TW, int TH>
+struct TileGeom {
+    static constexpr int VEC = VecT<T>::n;
+    int LP, RP, SW, SR;
+    __host__ __device__ TileGeom(const StencilArgs& a) {
+        LP = round_up_int(a.L, VEC);
+        RP = round_up_int(a.R, VEC);
+        SW = LP + TW + RP;
+        SR = TH + a.T + a.B;
+    }
+    __host__ __device__ size_t tile_bytes() const { return (size_t)SR * SW * sizeof(T); }
+    // tile | coefficients (ncoef T) | compact list offsets (ncoef int) | compact list weights (ncoef T)
+    __host__ __device__ size_t coef_off(const StencilArgs&) const { return round_up_int((int)tile_bytes(), 16); }
+    __host__ __device__ size_t list_off(const StencilArgs& a) const {
+        return coef_off(a) + round_up_int(a.ncoef * (int)sizeof(T), 16);
+    }
+    __host__ __device__ size_t listw_off(const StencilArgs& a) const {
+        return list_off(a) + round_up_int(a.ncoef * (int)sizeof(int), 16);
+    }
+    __host__ __device__ size_t total_bytes(const StencilArgs& a) const {
+        return listw_off(a) + round_up_int(a.ncoef * (int)sizeof(T), 16) + 16;
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ const T* launch_row(const StencilArgs& a, int gyl) {
+    // Launch-relative row gyl in [-T, rows + B): own rows, or the halo rows behind the top/bottom
+    // pointers (the per-tile boundaryTop/boundaryBottom pointers of the handle).
+    if (gyl >= 0 && gyl < a.rows) return reinterpret_cast<const T*>(a.in) + (size_t)gyl * a.nx;
+    if (gyl < 0) {
+        if (a.has_top && gyl + a.T >= 0) return reinterpret_cast<const T*>(a.top) + (size_t)(gyl + a.T) * a.nx;
+        return nullptr;
+    }
+    int k = gyl - a.rows;
+    if (a.has_bot && k < a.B) return reinterpret_cast<const T*>(a.bot) + (size_t)k * a.nx;
+    return nullptr;
+}
+
+// Stage coefficients and, for weight variants, the compact list of non-zero weights in weight order.
+template <typename T, int NT>
+__device__ __forceinline__ int stage_coefficients(const StencilArgs& a, T* coef_s, int* list_off, T* list_w,
+                                                  int SW, int tid, bool is_fun) {
+    const T* c = reinterpret_cast<const T*>(a.coef);
+    for (int k = tid; k < a.ncoef; k += NT) coef_s[k] = c[k];
+    __syncthreads();
+    __shared__ int s_count;
+    if (!is_fun && tid == 0) {
+        int n = 0;
+        for (int k = 0; k < a.ncoef; ++k) {
+            T w = coef_s[k];
+            if (w != T(0)) {
+                int j = k / a.H, i = k - j * a.H;
+                list_off[n] = j * SW + i;
+                list_w[n] = w;
+                ++n;
+            }
+        }
+        s_count = n;
+    }
+    __syncthreads();
+    return is_fun ? 0 : s_count;
+}
+
+// Plain-load staging of the window (16-byte vector loads where the whole vector is in range).
+template <typename T, int TW, int TH, int NT>
+__device__ __forceinline__ void stage_tile_ldg(const StencilArgs& a, T* tile, const TileGeom<T, TW, TH>& g,
+                                               int x0, int y0, int tid) {
+    constexpr int VEC = VecT<T>::n;
+    using V = typename VecT<T>::type;
+    const int cvecs = g.SW / VEC;
+    const int total = g.SR * cvecs;
+    for (int e = tid; e < total; e += NT) {
+        int r = e / cvecs;
+        int c = (e - r * cvecs) * VEC;
+        int gx = x0 - g.LP + c;
+        const T* rowp = launch_row<T>(a, y0 - a.T + r);
+        T* dst = tile + r * g.SW + c;
+        if (rowp == nullptr) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) dst[v] = T(0);
+            continue;
+        }
+        if (a.vec_ok && gx >= 0 && gx + VEC <= a.nx) {
+            *reinterpret_cast<V*>(dst) = __ldg(reinterpret_cast<const V*>(rowp + gx));
+        } else {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                int x = gx + v;
+                T val = T(0);
+                if (x >= 0 && x < a.nx) val = __ldg(rowp + x);
+                else if (a.wrap_x) {
+                    int xw = x < 0 ? x + a.nx : x - a.nx;
+                    if (xw >= 0 && xw < a.nx) val = __ldg(rowp + xw);
+                }
+                dst[v] = val;
+            }
+        }
+    }
+}
+
+template <typename T> using FunX = T (*)(T*, T*, int);
+template <typename T> using FunY = T (*)(T*, T*, int, int);
+template <typename T> using FunXY = T (*)(T*, T*, int, int, int, int);
+
+// Compute VEC x RPT outputs per thread from the staged window and store them.
+template <typename T, int TW, int TH, int RPT>
+__device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile, T* coef_s, const int* list_off,
+                                                  const T* list_w, int nlist, const TileGeom<T, TW, TH>& g,
+                                                  int x0, int y0, int tx, int ty, bool is_fun) {
+    constexpr int VEC = VecT<T>::n;
+    using V = typename VecT<T>::type;
+    const int c0 = tx * VEC;    // tile-local column of the first output
+    const int r0 = ty * RPT;    // tile-local row of the first output
+    T acc[RPT][VEC];
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr)
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) acc[rr][v] = T(0);
+
+    // Smem index of the top-left corner of the window of output (r0, c0).
+    const int base = r0 * g.SW + g.LP + c0 - a.L;
+    if (!is_fun) {
+        for (int e = 0; e < nlist; ++e) {
+            const T w = list_w[e];
+            const T* p = tile + base + list_off[e];
+#pragma unroll
+            for (int rr = 0; rr < RPT; ++rr)
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) acc[rr][v] = fma(w, p[rr * g.SW + v], acc[rr][v]);
+        }
+    } else {
+        const int dir = variant_dir(a.variant);
+#pragma unroll
+        for (int rr = 0; rr < RPT; ++rr) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                const int tl = base + rr * g.SW + v;    // window top-left
+                if (dir == 0) {
+                    acc[rr][v] = reinterpret_cast<FunX<T>>(a.func)(tile, coef_s, tl + a.L);
+                } else if (dir == 1) {
+                    acc[rr][v] = reinterpret_cast<FunY<T>>(a.func)(tile, coef_s, tl + a.T * g.SW + a.L, g.SW);
+                } else {
+                    acc[rr][v] = reinterpret_cast<FunXY<T>>(a.func)(tile, coef_s, tl, g.SW, a.H, a.V);
+                }
+            }
+        }
+    }
+
+    const int gx = x0 + c0;
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+        const int gyl = y0 + r0 + rr;
+        if (gyl >= a.rows) break;
+        const int gy = a.row0 + gyl;
+        T* orow = reinterpret_cast<T*>(a.out) + (size_t)gyl * a.nx;
+        int act[VEC];
+        bool all_write = true;
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) {
+            act[v] = (gx + v < a.nx) ? point_action(a.variant, gx + v, gy, a.nx, a.L, a.R, a.T, a.B, a.bx, a.by,
+                                                    a.nyTile, a.numTiles)
+                                     : ACT_SKIP;
+            all_write = all_write && (act[v] == ACT_WRITE);
+        }
+        if (all_write && a.vec_ok) {
+            V outv;
+            T* o = reinterpret_cast<T*>(&outv);
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) o[v] = acc[rr][v];
+            *reinterpret_cast<V*>(orow + gx) = outv;
+        } else {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                if (act[v] == ACT_WRITE) orow[gx + v] = acc[rr][v];
+                else if (act[v] == ACT_ZERO) orow[gx + v] = T(0);
+            }
+        }
+    }
+}
+
+}  // namespace custen

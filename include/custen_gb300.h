@@ -1,0 +1,130 @@
+/*
+ * custen_gb300.h -- C-ABI (extern "C") entry points of the GB300 cuSten rebuild.
+ *
+ * Every function returns 0 on success and a non-zero status otherwise (1: CUDA error, 2: invalid
+ * argument, 3: unsupported); custen_last_error() returns the message of the last failure on the
+ * calling thread. No function exits the process. Plain pointers and sizes only.
+ *
+ * The handle is the reference's own 200-byte cuSten_t (include/cuSten.h), allocated by the caller.
+ * Each create entry point takes the argument list of the reference function it mirrors (cited
+ * below, paths inside the cuSten project) and fills the handle exactly as the C++ drop-in API does;
+ * the _f32 forms take float data and run the FP32 kernels. Compute / swap / destroy dispatch on the
+ * variant recorded in the handle, so one entry point each replaces the reference's per-variant
+ * cuStenCompute2D* / cuStenSwap2D* / cuStenDestroy2D* functions.
+ */
+#ifndef CUSTEN_GB300_H
+#define CUSTEN_GB300_H
+
+#include <stddef.h>
+#include "cuSten.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Variant codes (the twelve operators of cuSten/src/kernels/stencil_kernels.h:52-183). */
+enum {
+    CUSTEN_XP = 0, CUSTEN_XNP = 1, CUSTEN_XPFUN = 2, CUSTEN_XNPFUN = 3,
+    CUSTEN_YP = 4, CUSTEN_YNP = 5, CUSTEN_YPFUN = 6, CUSTEN_YNPFUN = 7,
+    CUSTEN_XYP = 8, CUSTEN_XYNP = 9, CUSTEN_XYPFUN = 10, CUSTEN_XYNPFUN = 11
+};
+enum { CUSTEN_F64 = 0, CUSTEN_F32 = 1 };
+
+/* ---- library information ---- */
+int custen_abi_version(void);                 /* increments when an entry point changes */
+int custen_sizeof_handle(void);               /* sizeof(cuSten_t): 200 on LP64 */
+const char* custen_last_error(void);
+unsigned long long custen_kernel_launches(void);   /* kernels launched by this library so far */
+
+/* ---- handle life cycle: generic form ----
+ * H/L/R: window width and extents in x; V/T/B in y. X variants: V=1, T=B=0; Y variants: H=1, L=R=0.
+ * ncoef: number of weights/coefficients read per Compute. func: device function pointer (Fun). */
+int custen_create(cuSten_t* h, int variant, int dtype, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X,
+                  int BLOCK_Y, void* dataOutput, void* dataInput, void* coef, int H, int L, int R, int V, int T,
+                  int B, int ncoef, void* func);
+int custen_compute(cuSten_t* h, int offload);                       /* cuStenCompute2D*(h, offload) */
+int custen_compute_on_stream(cuSten_t* h, int offload, void* stream); /* same, all work on `stream` */
+int custen_swap(cuSten_t* h, void* dataInput);                      /* cuStenSwap2D*(h, dataInput) */
+int custen_destroy(cuSten_t* h);                                    /* cuStenDestroy2D*(h) */
+int custen_set_stream(cuSten_t* h, void* stream);   /* later Computes run on `stream` (NULL: own streams) */
+int custen_handle_variant(const cuSten_t* h, int* variant, int* dtype);
+
+/* ---- per-variant create, FP64, reference argument lists ---- */
+/* cuSten_struct_functions.h:184-198 */
+int custen_create_2d_xp(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                        double* dataOutput, double* dataInput, double* weights, int numSten, int numStenLeft,
+                        int numStenRight);
+/* :67-81 */
+int custen_create_2d_xnp(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                         double* dataOutput, double* dataInput, double* weights, int numSten, int numStenLeft,
+                         int numStenRight);
+/* :242-266 */
+int custen_create_2d_xp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                            double* dataOutput, double* dataInput, double* coe, int numSten, int numStenLeft,
+                            int numStenRight, int numCoe, double* func);
+/* :125-141 */
+int custen_create_2d_xnp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                             double* dataOutput, double* dataInput, double* coe, int numSten, int numStenLeft,
+                             int numStenRight, int numCoe, double* func);
+/* :742-756 */
+int custen_create_2d_yp(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                        double* dataOutput, double* dataInput, double* weights, int numSten, int numStenTop,
+                        int numStenBottom);
+/* :626-640 */
+int custen_create_2d_ynp(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                         double* dataOutput, double* dataInput, double* weights, int numSten, int numStenTop,
+                         int numStenBottom);
+/* :801-817 */
+int custen_create_2d_yp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                            double* dataOutput, double* dataInput, double* coe, int numSten, int numStenTop,
+                            int numStenBottom, int numCoe, double* func);
+/* :684-699 (no numCoe; numSten coefficients are read) */
+int custen_create_2d_ynp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                             double* dataOutput, double* dataInput, double* coe, int numSten, int numStenTop,
+                             int numStenBottom, double* func);
+/* :500-517 */
+int custen_create_2d_xyp(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                         double* dataOutput, double* dataInput, double* weights, int numStenHoriz, int numStenLeft,
+                         int numStenRight, int numStenVert, int numStenTop, int numStenBottom);
+/* :371-388 */
+int custen_create_2d_xynp(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                          double* dataOutput, double* dataInput, double* weights, int numStenHoriz, int numStenLeft,
+                          int numStenRight, int numStenVert, int numStenTop, int numStenBottom);
+/* :564-582 */
+int custen_create_2d_xyp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                             double* dataOutput, double* dataInput, double* coe, int numStenHoriz, int numStenLeft,
+                             int numStenRight, int numStenVert, int numStenTop, int numStenBottom, double* func);
+/* :435-453 */
+int custen_create_2d_xynp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
+                              double* dataOutput, double* dataInput, double* coe, int numStenHoriz, int numStenLeft,
+                              int numStenRight, int numStenVert, int numStenTop, int numStenBottom, double* func);
+
+/* ---- device functions shipped with the library for the Fun variants ----
+ * id 0: X  (d[l-1] - 2 d[l] + d[l+1]) * coe[0]
+ *         (the user function of the reference example examples/src/2d_x_np_fun.cu:49-51)
+ * id 1: X  sum_k coe[k] * (d^3 - d) over the window l-L..l+R, L = R = 2 (5 coefficients)
+ * id 2: Y  sum_k coe[k] * d[l + (k-4)*jump], 9 coefficients (examples/src/2d_y_p_fun.cu:49-60)
+ * id 3: Y  sum_k coe[k] * (d^3 - d) over rows l-2..l+2 (5 coefficients)
+ * id 4: XY sum_{j,i} coe[j*H+i] * d[tl + j*jump + i] (examples/src/2d_xy_p_fun.cu:58-80)
+ * id 5: XY sum_{j,i} coe[j*H+i] * (d^3 - d) (the Cahn-Hilliard nonLinRHS,
+ *         cuPentCahnADI/src/cuPentCahnADI.cu:164-190)
+ * All use explicit fused multiply-adds in a fixed order, so their results are reproducible on the
+ * host. `dtype` selects the double or float version. */
+int custen_builtin_function(int id, int dtype, void** func);
+
+/* ---- memory helpers for hosts without a CUDA runtime binding ---- */
+int custen_malloc_managed(void** ptr, size_t bytes);
+int custen_malloc_device(void** ptr, size_t bytes);
+int custen_malloc_host(void** ptr, size_t bytes);    /* pinned */
+int custen_free(void* ptr);
+int custen_free_host(void* ptr);
+int custen_memcpy(void* dst, const void* src, size_t bytes);   /* cudaMemcpyDefault, synchronous */
+int custen_memset(void* ptr, int value, size_t bytes);
+int custen_device_synchronize(void);
+int custen_set_device(int device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUSTEN_GB300_H */

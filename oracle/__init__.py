@@ -1,0 +1,87 @@
+"""Oracles -- TEST INFRASTRUCTURE ONLY (used by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg as the checker; never by the library).
+
+* ``stencil_oracle.c``: C restatement of the twelve cuSten stencil kernels (block-by-block emulation,
+  see the header of that file).
+* ``ch_oracle.c``: C restatement of the Cahn-Hilliard ADI solver of
+  cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c.
+* ``ref_build.py``: builds the reference's own code from the reference sources into ``oracle/_ref``
+  (the serial Cahn-Hilliard program as a shared library, and the cuSten kernels as an sm_103a cubin);
+  only possible where the reference sources are present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+LIB = BUILD / "liboracle.so"
+SOURCES = [HERE / "stencil_oracle.c", HERE / "ch_oracle.c"]
+HEADERS = [HERE / "stencil_oracle_impl.h"]
+
+_lib = None
+
+
+def build() -> Path:
+    """Compile the C oracles (gcc, contraction off so that every fma is explicit)."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    srcs = [s for s in SOURCES if s.exists()]
+    deps = srcs + HEADERS
+    if not LIB.exists() or any(d.stat().st_mtime > LIB.stat().st_mtime for d in deps):
+        tmp = LIB.with_suffix(".so.tmp")
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-o", str(tmp),
+               *map(str, srcs), "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB))
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        for name in ("oracle_stencil_f64", "oracle_stencil_f32"):
+            f = getattr(L, name)
+            f.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, i, vp]
+            f.restype = i
+        L.oracle_host_loop_xyp_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def stencil(variant: int, out: np.ndarray, inp: np.ndarray, coef: np.ndarray, *, num_tiles: int, block_x: int,
+            block_y: int, H: int, L: int, R: int, V: int, T: int, B: int, fun_id: int = -1,
+            halo_src: np.ndarray | None = None) -> np.ndarray:
+    """One Compute of `variant`; `out` (ny x nx) is updated in place. Returns the status array
+    (0 untouched, 1 written, 2 written from shared memory the reference never loaded)."""
+    assert out.dtype == inp.dtype == coef.dtype and out.flags.c_contiguous and inp.flags.c_contiguous
+    ny, nx = inp.shape
+    status = np.zeros((ny, nx), dtype=np.uint8)
+    fn = lib().oracle_stencil_f64 if inp.dtype == np.float64 else lib().oracle_stencil_f32
+    coef = np.ascontiguousarray(coef)
+    rc = fn(variant, nx, ny, num_tiles, block_x, block_y, _p(out), _p(inp), _p(halo_src), _p(coef), coef.size, H, L,
+            R, V, T, B, fun_id, _p(status))
+    if rc != 0:
+        raise ValueError("configuration outside the reference kernels' contract")
+    return status
+
+
+def host_loop_xyp(inp: np.ndarray, w: np.ndarray, H: int, L: int, V: int, T: int, y0: int = 0,
+                  y1: int | None = None) -> np.ndarray:
+    """Plain periodic host loop (CPU baseline), rows [y0, y1)."""
+    ny, nx = inp.shape
+    out = np.zeros_like(inp)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    lib().oracle_host_loop_xyp_f64(nx, ny, _p(inp), _p(out), _p(w), H, L, V, T, y0, ny if y1 is None else y1)
+    return out

@@ -1,0 +1,199 @@
+"""Parity of the sm_103a stencil kernels with the oracle (GPU).
+
+Every written point must be bit-identical to the oracle's FMA chain; every point the reference leaves
+untouched must keep the sentinel it was pre-filled with; points the reference writes from shared
+memory it never loaded (oracle status 2) are left untouched by this library.
+"""
+import numpy as np
+import pytest
+
+import custen_gb300 as cs
+import oracle
+from tests.helpers import DeviceBuffer, field, sentinel, weights_for
+
+pytestmark = pytest.mark.gpu
+
+FUN_IDS = {0: (0, 1), 1: (2, 3), 2: (4, 5)}  # shipped device functions per direction
+
+
+def geometry(variant, kind):
+    """(H, L, R, V, T, B) for a direction and a halo shape."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    shapes = {
+        0: {"sym": (5, 2, 2, 1, 0, 0), "asym": (5, 3, 1, 1, 0, 0), "small": (3, 1, 1, 1, 0, 0)},
+        1: {"sym": (1, 0, 0, 5, 2, 2), "asym": (1, 0, 0, 5, 1, 3), "small": (1, 0, 0, 3, 1, 1)},
+        2: {"sym": (5, 2, 2, 5, 2, 2), "asym": (4, 2, 1, 3, 1, 1), "small": (3, 1, 1, 3, 1, 1)},
+    }
+    return shapes[d][kind]
+
+
+def run_both(variant, nx, ny, tiles, bx, by, geom, dtype=np.float64, fun_id=-1, seed=0, managed=False,
+             offload=cs.DEVICE):
+    H, L, R, V, T, B = geom
+    inp = field(nx, ny, seed, dtype)
+    fun = fun_id >= 0
+    if fun:
+        ncoef = {0: 1, 1: 5, 2: 9, 3: 5, 4: H * V, 5: H * V}[fun_id]
+        coef = np.random.default_rng(50 + seed).uniform(-1, 1, ncoef).astype(dtype)
+    else:
+        coef = weights_for(variant, H, V, seed, dtype)
+        ncoef = coef.size
+    pre = sentinel(nx, ny, dtype)
+    ref = pre.copy()
+    st = oracle.stencil(variant, ref, inp, coef, num_tiles=tiles, block_x=bx, block_y=by, H=H, L=L, R=R, V=V, T=T,
+                        B=B, fun_id=fun_id)
+
+    dt = cs.F64 if dtype == np.float64 else cs.F32
+    d_in = DeviceBuffer.from_array(inp, managed)
+    d_out = DeviceBuffer.from_array(pre, managed)
+    d_c = DeviceBuffer.from_array(coef, managed)
+    func = cs.builtin_function(fun_id, dt) if fun else None
+    s = cs.Stencil(variant, nx, ny, d_out.ptr, d_in.ptr, d_c.ptr, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=tiles,
+                   block_x=bx, block_y=by, dtype=dt, ncoef=ncoef, func=func)
+    s.compute(offload)
+    cs._check(cs.lib().custen_device_synchronize())
+    got = d_out.view((ny, nx), dtype).copy() if managed else d_out.download((ny, nx), dtype)
+    s.destroy()
+    return got, ref, st, pre
+
+
+def check(got, ref, st, pre):
+    w = st == 1
+    bad = w & ~((got == ref) | (np.isnan(got) & np.isnan(ref)))
+    assert not bad.any(), f"{bad.sum()} written points differ; first at {np.argwhere(bad)[:3].tolist()}"
+    keep = st != 1
+    assert np.array_equal(got[keep], pre[keep]), "points the reference leaves untouched were modified"
+
+
+VARIANTS = list(range(12))
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=cs.VARIANT_NAMES)
+@pytest.mark.parametrize("tiles", [1, 2, 4])
+@pytest.mark.parametrize("kind", ["sym", "asym"])
+def test_parity_f64(gpu, variant, tiles, kind):
+    geom = geometry(variant, kind)
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    fun = variant in (cs.XPFUN, cs.XNPFUN, cs.YPFUN, cs.YNPFUN, cs.XYPFUN, cs.XYNPFUN)
+    fun_id = -1
+    if fun:
+        fun_id = FUN_IDS[d][1]           # the (c^3 - c) functions reach 2 points
+        if d == 1:
+            geom = (1, 0, 0, 5, 2, 2)
+        elif d == 0:
+            geom = (5, 2, 2, 1, 0, 0)
+    nx, ny = (96, 64) if d != 1 else (48, 128)
+    got, ref, st, pre = run_both(variant, nx, ny, tiles, 32 if d != 1 else 16, 8, geom, fun_id=fun_id,
+                                 seed=variant * 7 + tiles)
+    check(got, ref, st, pre)
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=cs.VARIANT_NAMES)
+def test_parity_f32(gpu, variant):
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    fun = variant in (cs.XPFUN, cs.XNPFUN, cs.YPFUN, cs.YNPFUN, cs.XYPFUN, cs.XYNPFUN)
+    geom = geometry(variant, "sym")
+    fun_id = FUN_IDS[d][1] if fun else -1
+    nx, ny = (128, 64) if d != 1 else (64, 128)
+    got, ref, st, pre = run_both(variant, nx, ny, 2, 32, 8, geom, dtype=np.float32, fun_id=fun_id, seed=variant)
+    check(got, ref, st, pre)
+
+
+@pytest.mark.parametrize("variant", [cs.XP, cs.XNP, cs.YP, cs.YNP, cs.XYP, cs.XYNP])
+def test_parity_unaligned_rows(gpu, variant):
+    """nx = 98 doubles: rows are not 16-byte aligned, the scalar staging/store path runs."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    got, ref, st, pre = run_both(variant, 98, 56, 2, 14, 4, geometry(variant, "small"), seed=11)
+    check(got, ref, st, pre)
+
+
+@pytest.mark.parametrize("variant", [cs.XPFUN, cs.YPFUN, cs.XYPFUN, cs.XNPFUN, cs.YNPFUN, cs.XYNPFUN])
+def test_parity_reference_example_functions(gpu, variant):
+    """The example user functions: X 3-point (id 0), Y 9-point (id 2), XY weighted window (id 4)."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    geom = {0: (3, 1, 1, 1, 0, 0), 1: (1, 0, 0, 9, 4, 4), 2: (3, 1, 1, 3, 1, 1)}[d]
+    fun_id = FUN_IDS[d][0]
+    nx, ny = (64, 64) if d != 1 else (32, 128)
+    got, ref, st, pre = run_both(variant, nx, ny, 2, 16 if d != 1 else 8, 8, geom, fun_id=fun_id, seed=3)
+    check(got, ref, st, pre)
+
+
+@pytest.mark.parametrize("variant", [cs.XP, cs.YNP, cs.XYP, cs.XYNPFUN])
+def test_managed_memory_tile_streaming(gpu, variant):
+    """Managed memory, numTiles = 4, HOST offload: tiles stream through the GPU and come back."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    fun_id = FUN_IDS[d][1] if variant == cs.XYNPFUN else -1
+    got, ref, st, pre = run_both(variant, 64, 128, 4, 16, 8, geometry(variant, "sym"), fun_id=fun_id, seed=5,
+                                 managed=True, offload=cs.HOST)
+    check(got, ref, st, pre)
+
+
+@pytest.mark.parametrize("variant", [cs.YP, cs.XYP, cs.YNP, cs.XYNP])
+def test_swap_sequence(gpu, variant):
+    """Create(out=A, in=B); Compute; Swap(A); Compute: the second Compute reads A and writes B, with
+    the halo pointers recomputed from the Swap argument (custenCreateDestroy2DYp.cu:235-283)."""
+    nx, ny, tiles, bx, by = 64, 96, 3, 16, 8
+    H, L, R, V, T, B = geometry(variant, "sym")
+    a0 = field(nx, ny, 21)
+    w = weights_for(variant, H, V, 4)
+    A = sentinel(nx, ny)
+    Bf = a0.copy()
+    dA, dB, dw = DeviceBuffer.from_array(A), DeviceBuffer.from_array(Bf), DeviceBuffer.from_array(w)
+    s = cs.Stencil(variant, nx, ny, dA.ptr, dB.ptr, dw.ptr, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=tiles,
+                   block_x=bx, block_y=by)
+    s.compute()
+    s.swap(dA.ptr)
+    s.compute()
+    cs._check(cs.lib().custen_device_synchronize())
+    gotA, gotB = dA.download((ny, nx), np.float64), dB.download((ny, nx), np.float64)
+    s.destroy()
+    refA = A.copy()
+    oracle.stencil(variant, refA, Bf, w, num_tiles=tiles, block_x=bx, block_y=by, H=H, L=L, R=R, V=V, T=T, B=B)
+    refB = Bf.copy()
+    oracle.stencil(variant, refB, refA, w, num_tiles=tiles, block_x=bx, block_y=by, H=H, L=L, R=R, V=V, T=T, B=B)
+    assert np.array_equal(gotA, refA)
+    assert np.array_equal(gotB, refB)
+
+
+@pytest.mark.parametrize("variant", [cs.YP, cs.XYP])
+def test_swap_with_foreign_halo_source(gpu, variant):
+    """Swap(h, C) with C not the new input: the halo rows of every tile come from C, as in the
+    reference (the tiles are then not contiguous with their halos and run one launch each)."""
+    nx, ny, tiles, bx, by = 64, 64, 2, 16, 8
+    H, L, R, V, T, B = geometry(variant, "sym")
+    a0, c0 = field(nx, ny, 31), field(nx, ny, 32)
+    w = weights_for(variant, H, V, 9)
+    A = sentinel(nx, ny)
+    dA, dB, dC, dw = (DeviceBuffer.from_array(A), DeviceBuffer.from_array(a0), DeviceBuffer.from_array(c0),
+                      DeviceBuffer.from_array(w))
+    s = cs.Stencil(variant, nx, ny, dA.ptr, dB.ptr, dw.ptr, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=tiles,
+                   block_x=bx, block_y=by)
+    s.swap(dC.ptr)           # now in = A, out = B, halos from C
+    dA.upload(a0)
+    s.compute()
+    cs._check(cs.lib().custen_device_synchronize())
+    got = dB.download((ny, nx), np.float64)
+    s.destroy()
+    ref = a0.copy()
+    oracle.stencil(variant, ref, a0, w, num_tiles=tiles, block_x=bx, block_y=by, H=H, L=L, R=R, V=V, T=T, B=B,
+                   halo_src=c0)
+    assert np.array_equal(got, ref)
+
+
+def test_weights_reread_every_compute(gpu):
+    """Weights are read from memory on every Compute (2d_x_p_kernel.cu:79-83)."""
+    nx, ny = 64, 32
+    inp = field(nx, ny, 2)
+    w1 = np.array([1.0, -2.0, 1.0])
+    w2 = np.array([0.5, 0.25, -3.0])
+    d_in, d_out, d_w = DeviceBuffer.from_array(inp), DeviceBuffer.from_array(np.zeros_like(inp)), DeviceBuffer.from_array(w1)
+    s = cs.Stencil(cs.XP, nx, ny, d_out.ptr, d_in.ptr, d_w.ptr, H=3, L=1, R=1)
+    s.compute()
+    d_w.upload(w2)
+    s.compute()
+    cs._check(cs.lib().custen_device_synchronize())
+    got = d_out.download((ny, nx), np.float64)
+    s.destroy()
+    ref = np.zeros_like(inp)
+    oracle.stencil(cs.XP, ref, inp, w2, num_tiles=1, block_x=32, block_y=8, H=3, L=1, R=1, V=1, T=0, B=0)
+    assert np.array_equal(got, ref)
