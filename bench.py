@@ -1,0 +1,450 @@
+#!/usr/bin/env python
+"""Benchmark: the cuSten plain stencil sweep, FP64, on GB300.
+
+One step = one Compute of each of the twelve cuSten operators on an n x n field (default 16384^2):
+X and Y 5-point 4th-order d2/dx2 [-1,16,-30,16,-1]/(12h^2) (periodic and non-periodic), XY 3x3
+cross-derivative [1,0,-1;0,0,0;-1,0,1]/(4h^2) (p, np), and the Fun variants applying c^3 - c before
+the same stencil (X, Y 5-point; XY 3x3 5-point Laplacian [0,1,0;1,-4,1;0,1,0]/h^2), all with numTiles=1
+on device-resident data. Input sin(3x)cos(5y) + U(-1e-3, 1e-3) from seed 1 (synthetic).
+Metric: Gpts/s = 12 * n^2 points per step / step time. Every field (2 GiB) is larger than L2.
+
+Extra keys: per-operator Gpts/s; roofline of the stencil kernel against measured HBM bandwidth and
+against the measured FP64 FMA rate (the FP64 kernels are FP64-pipe bound on GB300); the FP32
+precision variant (same sweep in FP32 with its error against FP64); e2e through the reference-facing
+API with host (managed) buffers, numTiles=4 and HOST offload; and the CPU baseline (plain host loop,
+same weights and FMA order, all host threads, bounded row sample).
+
+--impl reference: the reference has no CPU stencil implementation, so the reference arm times the
+plain host loop port (oracle) on the same workload sample; it prints the same JSON keys.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+W5 = [-1.0, 16.0, -30.0, 16.0, -1.0]
+WCROSS = [1.0, 0.0, -1.0, 0.0, 0.0, 0.0, -1.0, 0.0, 1.0]
+WLAP = [0.0, 1.0, 0.0, 1.0, -4.0, 1.0, 0.0, 1.0, 0.0]
+
+
+def operators(n: int):
+    """(name, variant, H, L, R, V, T, B, weights, fun_id, dfma_per_point)"""
+    h = 2 * math.pi / n
+    w5 = [w / (12 * h * h) for w in W5]
+    wc = [w / (4 * h * h) for w in WCROSS]
+    wl = [w / (h * h) for w in WLAP]
+    # FP64 operations per point: weights skip exact zeros; Fun variants apply c^3-c (mul + fma) per
+    # window point and an fma per coefficient (zeros included: the user function decides).
+    ops = []
+    for nm, v in (("Xp", 0), ("Xnp", 1)):
+        ops.append((nm, v, 5, 2, 2, 1, 0, 0, w5, -1, 5))
+    for nm, v in (("XpFun", 2), ("XnpFun", 3)):
+        ops.append((nm, v, 5, 2, 2, 1, 0, 0, w5, 1, 15))
+    for nm, v in (("Yp", 4), ("Ynp", 5)):
+        ops.append((nm, v, 1, 0, 0, 5, 2, 2, w5, -1, 5))
+    for nm, v in (("YpFun", 6), ("YnpFun", 7)):
+        ops.append((nm, v, 1, 0, 0, 5, 2, 2, w5, 3, 15))
+    for nm, v in (("XYp", 8), ("XYnp", 9)):
+        ops.append((nm, v, 3, 1, 1, 3, 1, 1, wc, -1, 4))
+    for nm, v in (("XYpFun", 10), ("XYnpFun", 11)):
+        ops.append((nm, v, 3, 1, 1, 3, 1, 1, wl, 5, 27))
+    return ops
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+# ----------------------------------------------------------------------------------------------
+# CPU leg: plain host loop (oracle port), all host threads, bounded row sample
+# ----------------------------------------------------------------------------------------------
+def cpu_sample(n: int, rows: int, threads: int):
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    import oracle
+    from tests.helpers import field
+    oracle.build()
+    # rows sampled from the real n x n field: build only the rows the sample reads (+ halos)
+    full_rows = rows + 4
+    rng_field = field(n, full_rows, 1)   # same generator, shape (full_rows, n)
+    out = np.zeros_like(rng_field)
+    ops = operators(n)
+
+    def one_pass():
+        pts = 0
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            futs = []
+            chunk = max(1, rows // threads)
+            for (_, v, H, L, R, V, T, B, w, fun, _) in ops:
+                for y0 in range(2, 2 + rows, chunk):
+                    y1 = min(2 + rows, y0 + chunk)
+                    futs.append(ex.submit(oracle.host_loop, rng_field, out, np.asarray(w), H, L, V, T, fun >= 0,
+                                          y0, y1))
+                pts += rows * n
+            for f in futs:
+                f.result()
+        return pts
+
+    return one_pass
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rows = args.cpu_rows
+    one = cpu_sample(args.n, rows, threads)
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    pts = 0
+    for _ in range(args.steps):
+        pts += one()
+    dt = time.perf_counter() - t0
+    v = pts / dt / 1e9
+    line = {
+        "impl": "reference", "metric": "stencil Gpts/s", "value": round(v, 4), "unit": "Gpts/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"stencil sweep FP64 {args.n}^2, 12 cuSten operators (sample of {rows} rows each)",
+                   "nx": args.n, "ny": args.n},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Gpts/s", "cores": threads, "kind": "port",
+                         "sample": f"{rows} rows x {args.n} columns per operator, 12 operators, plain host loop"},
+        "e2e": {"value": round(v, 4), "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------------------------
+def run_gpu(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import custen_gb300 as cs
+
+    cs.build()
+    torch.cuda.set_device(local)
+    cs._check(cs.lib().custen_set_device(local))
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    n = args.n
+    ops = operators(n)
+    stream = torch.cuda.current_stream(dev)
+
+    def make_field(dtype):
+        x = torch.arange(n, device=dev, dtype=torch.float64) * (2 * math.pi / n)
+        g = torch.Generator(device=dev)
+        g.manual_seed(1)
+        f = torch.sin(3 * x)[None, :] * torch.cos(5 * x)[:, None]
+        f = f + (torch.rand((n, n), device=dev, dtype=torch.float64, generator=g) * 2e-3 - 1e-3)
+        return f.to(dtype).contiguous()
+
+    def build_handles(dtype_t, cs_dtype, num_tiles=1, managed=False):
+        inp = make_field(dtype_t)
+        outs, hs, keep = [], [], []
+        for (nm, v, H, L, R, V, T, B, w, fun, _) in ops:
+            wt = torch.tensor(w, device=dev, dtype=dtype_t)
+            o = torch.zeros((n, n), device=dev, dtype=dtype_t)
+            func = cs.builtin_function(fun, cs_dtype) if fun >= 0 else None
+            h = cs.Stencil(v, n, n, o, inp, wt, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=num_tiles, block_x=32,
+                           block_y=8, dtype=cs_dtype, device=local, ncoef=len(w), func=func)
+            h.set_stream(stream)
+            outs.append(o)
+            hs.append(h)
+            keep.append(wt)
+        return inp, outs, hs, keep
+
+    def timed_sweep(hs, steps, warmup):
+        for _ in range(warmup):
+            for h in hs:
+                h.compute()
+        torch.cuda.synchronize(dev)
+        if pg:
+            pg.barrier()
+        ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in hs]
+              for _ in range(steps)]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        launches0 = cs.kernel_launches()
+        torch.cuda.synchronize(dev)
+        t0.record(stream)
+        for s in range(steps):
+            for k, h in enumerate(hs):
+                ev[s][k][0].record(stream)
+                h.compute()
+                ev[s][k][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        launches = cs.kernel_launches() - launches0
+        total_ms = t0.elapsed_time(t1)
+        per_op = [sum(ev[s][k][0].elapsed_time(ev[s][k][1]) for s in range(steps)) / steps for k in range(len(hs))]
+        return total_ms, per_op, launches
+
+    # ---- FP64 sweep (headline) ----
+    inp64, outs64, hs64, keep64 = build_handles(torch.float64, cs.F64)
+    sampler = ClockSampler(local)
+    sampler.start()
+    total_ms, per_op, launches = timed_sweep(hs64, args.steps, args.warmup)
+    clocks = sampler.stop()
+    if pg:
+        t = torch.tensor([total_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    pts_step = len(ops) * n * n
+    value = world * pts_step / (ms_per_step * 1e-3) / 1e9
+
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    hbm_src = "measured" if peaks.get("hbm_gbs") else "fallback"
+    kernel_ms = sum(per_op)
+    bytes_alg = 16.0 * n * n * len(ops)
+    achieved_gbs = bytes_alg / (kernel_ms * 1e-3) / 1e9
+    fp64_rate = cs.probe_fma_rate(cs.F64)
+    dfma = sum(o[10] for o in ops) * n * n
+    achieved_fma = dfma / (kernel_ms * 1e-3)
+
+    per = {}
+    for (nm, v, *_rest), ms in zip(ops, per_op):
+        dfma_pt = _rest[-1]
+        per[nm] = {"gpts_s": round(n * n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 4),
+                   "hbm_gbs": round(16.0 * n * n / (ms * 1e-3) / 1e9, 1),
+                   "fp64_frac": round(dfma_pt * n * n / (ms * 1e-3) / fp64_rate, 3)}
+
+    # ---- FP32 precision variant: same sweep in FP32, error against the FP64 outputs ----
+    fp32 = None
+    if not args.skip_fp32:
+        inp32, outs32, hs32, keep32 = build_handles(torch.float32, cs.F32)
+        ms32, per32, _ = timed_sweep(hs32, max(1, args.steps), 3)
+        fp32 = {"gpts_s": round(pts_step / (ms32 / max(1, args.steps) * 1e-3) / 1e9, 3),
+                "hbm_gbs": round(8.0 * pts_step / (sum(per32) * 1e-3) / 1e9, 1), "per_op": {}}
+        for (nm, *_r), ms, o32, o64 in zip(ops, per32, outs32, outs64):
+            d = o32.double() - o64
+            fp32["per_op"][nm] = {
+                "gpts_s": round(n * n / (ms * 1e-3) / 1e9, 3),
+                "gbs": round(8.0 * n * n / (ms * 1e-3) / 1e9, 1),
+                "max_abs_err": float(d.abs().max().item()),
+                "rel_l2": float((d.norm() / o64.norm()).item()),
+            }
+        del inp32, outs32, hs32, keep32
+        torch.cuda.synchronize(dev)
+
+    # ---- e2e: reference-facing API with host buffers (managed memory, numTiles=4, HOST offload) ----
+    e2e = None
+    if not args.skip_e2e:
+        e2e = run_e2e(args, cs, np, local, ops)
+
+    # ---- CPU baseline (rank 0 only) ----
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        one = cpu_sample(n, args.cpu_rows, threads)
+        one()
+        t0c = time.perf_counter()
+        pts = one()
+        dtc = time.perf_counter() - t0c
+        cpu = {"value": round(pts / dtc / 1e9, 4), "unit": "Gpts/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_rows} rows x {n} columns per operator, 12 operators, plain host loop, "
+                         f"{threads} threads"}
+
+    for h in hs64:
+        h.destroy()
+
+    if rank == 0:
+        line = {
+            "metric": "stencil Gpts/s", "value": round(value, 3), "unit": "Gpts/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: sin(3x)cos(5y)+U(-1e-3,1e-3), seed 1",
+            "config": {"workload": f"cuSten stencil sweep FP64 {n}^2: 12 operators (X/Y 5-pt p/np, XY 3x3 "
+                                   f"cross p/np, Fun c^3-c X/Y/XY p/np), numTiles=1, device-resident",
+                       "nx": n, "ny": n, "numTiles": 1, "l2": "inputs larger than L2 (2 GiB per field)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": round(achieved_gbs / hbm_peak, 4), "traffic": args.traffic,
+                         "peak_source": f"{hbm_src} hbm_gbs",
+                         "note": "16 B/pt algorithmic; FP64 kernels are bound by the FP64 FMA pipe, see fp64"},
+            "fp64": {"achieved_fma_s": round(achieved_fma / 1e9, 1), "peak_fma_s": round(fp64_rate / 1e9, 1),
+                     "unit": "G FMA/s", "frac": round(achieved_fma / fp64_rate, 4),
+                     "peak_source": "measured live (custen_probe_fma_rate)"},
+            "per_op": per,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        if fp32 is not None:
+            line["fp32"] = fp32
+        if e2e is not None:
+            line["e2e"] = e2e
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+def run_e2e(args, cs, np, local, ops):
+    """Same sweep through the reference-facing API on host (managed) buffers: numTiles=4, HOST offload.
+    Each Compute streams its tiles to the GPU and back (cudaMemPrefetchAsync), inside the timed region."""
+    import ctypes
+
+    n = args.e2e_n
+    nbytes = n * n * 8
+    lib = cs.lib()
+
+    def managed(nb):
+        p = ctypes.c_void_p()
+        cs._check(lib.custen_malloc_managed(ctypes.byref(p), nb))
+        return p.value
+
+    from tests.helpers import field
+    inp = managed(nbytes)
+    arr = np.frombuffer((ctypes.c_char * nbytes).from_address(inp), dtype=np.float64).reshape(n, n)
+    arr[:] = field(n, n, 1)
+    outs, hs, ws = [], [], []
+    for (nm, v, H, L, R, V, T, B, w, fun, _) in ops:
+        o = managed(nbytes)
+        np.frombuffer((ctypes.c_char * nbytes).from_address(o), dtype=np.float64)[:] = 0.0
+        wp = managed(8 * len(w))
+        np.frombuffer((ctypes.c_char * (8 * len(w))).from_address(wp), dtype=np.float64)[:] = w
+        func = cs.builtin_function(fun, cs.F64) if fun >= 0 else None
+        hs.append(cs.Stencil(v, n, n, o, inp, wp, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=4, block_x=32, block_y=8,
+                             ncoef=len(w), func=func, device=local))
+        outs.append(o)
+        ws.append(wp)
+    for h in hs:
+        h.compute(cs.HOST)
+    cs._check(lib.custen_device_synchronize())
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        for h in hs:
+            h.compute(cs.HOST)
+        cs._check(lib.custen_device_synchronize())
+        _ = float(np.frombuffer((ctypes.c_char * 8).from_address(outs[-1]), dtype=np.float64)[0])  # host read
+    dt = (time.perf_counter() - t0) / args.e2e_steps
+    for h in hs:
+        h.destroy()
+    for p in outs + ws + [inp]:
+        lib.custen_free(p)
+    per_compute = 2 * nbytes   # input and output tiles to the device, then both back
+    return {"value": round(len(ops) * n * n / dt / 1e9, 3), "unit": "Gpts/s",
+            "h2d_bytes_per_step": per_compute * len(ops), "d2h_bytes_per_step": per_compute * len(ops),
+            "path": f"managed host buffers {n}^2, numTiles=4, Compute(HOST) per operator (tile streaming)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--e2e-n", type=int, default=16384)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-rows", type=int, default=4096)
+    ap.add_argument("--skip-fp32", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="dram bytes per launch from an ncu capture (recorded in the roofline object)")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+    run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

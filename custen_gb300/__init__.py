@@ -64,6 +64,7 @@ def lib() -> ctypes.CDLL:
         L.custen_memcpy.argtypes = [vp, vp, sz]
         L.custen_memset.argtypes = [vp, i, sz]
         L.custen_set_device.argtypes = [i]
+        L.custen_probe_fma_rate.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
         _lib = L
     return _lib
 
@@ -93,6 +94,13 @@ def builtin_function(fid: int, dtype: int = F64) -> int:
     p = ctypes.c_void_p()
     _check(lib().custen_builtin_function(fid, dtype, ctypes.byref(p)))
     return int(p.value)
+
+
+def probe_fma_rate(dtype: int = F64) -> float:
+    """Measured FMA/s of this GPU (all SMs, independent chains)."""
+    r = ctypes.c_double()
+    _check(lib().custen_probe_fma_rate(dtype, ctypes.byref(r)))
+    return float(r.value)
 
 
 def kernel_launches() -> int:

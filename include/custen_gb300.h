@@ -8,7 +8,8 @@
  * The handle is the reference's own 200-byte cuSten_t (include/cuSten.h), allocated by the caller.
  * Each create entry point takes the argument list of the reference function it mirrors (cited
  * below, paths inside the cuSten project) and fills the handle exactly as the C++ drop-in API does;
- * the _f32 forms take float data and run the FP32 kernels. Compute / swap / destroy dispatch on the
+ * custen_create with dtype CUSTEN_F32 takes float data and runs the FP32 kernels (the precision
+ * variant; the reference is FP64 only). Compute / swap / destroy dispatch on the
  * variant recorded in the handle, so one entry point each replaces the reference's per-variant
  * cuStenCompute2D* / cuStenSwap2D* / cuStenDestroy2D* functions.
  */
@@ -111,6 +112,11 @@ int custen_create_2d_xynp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, 
  * All use explicit fused multiply-adds in a fixed order, so their results are reproducible on the
  * host. `dtype` selects the double or float version. */
 int custen_builtin_function(int id, int dtype, void** func);
+
+/* ---- measurement ----
+ * Sustained FMA rate of this GPU (FMA per second, 8 independent chains per thread, all SMs), the
+ * compute-roofline denominator of the FP64 stencils. No counterpart in the reference. */
+int custen_probe_fma_rate(int dtype, double* fma_per_s);
 
 /* ---- memory helpers for hosts without a CUDA runtime binding ---- */
 int custen_malloc_managed(void** ptr, size_t bytes);

@@ -24,7 +24,27 @@ LIB = BUILD / "liboracle.so"
 SOURCES = [HERE / "stencil_oracle.c", HERE / "ch_oracle.c"]
 HEADERS = [HERE / "stencil_oracle_impl.h"]
 
+REFRUN = BUILD / "librefrun.so"
+REF_CUBIN = HERE / "_ref" / "custen_ref_sm103a.cubin"
+CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+
 _lib = None
+_refrun = None
+
+
+def _build_refrun() -> None:
+    src = HERE / "ref_runner.cpp"
+    if REFRUN.exists() and REFRUN.stat().st_mtime >= src.stat().st_mtime:
+        return
+    tmp = REFRUN.with_suffix(".so.tmp")
+    libdirs = [CUDA_HOME / "lib64", CUDA_HOME / "lib64" / "stubs", CUDA_HOME / "targets" / "sbsa-linux" / "lib" / "stubs"]
+    cmd = ["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-I", str(CUDA_HOME / "include"), "-o", str(tmp), str(src)]
+    for d in libdirs:
+        if d.exists():
+            cmd += ["-L", str(d)]
+    cmd += ["-lcuda"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, REFRUN)
 
 
 def build() -> Path:
@@ -38,6 +58,7 @@ def build() -> Path:
                *map(str, srcs), "-lm"]
         subprocess.run(cmd, check=True)
         os.replace(tmp, LIB)
+    _build_refrun()
     return LIB
 
 
@@ -52,6 +73,7 @@ def lib() -> ctypes.CDLL:
             f.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, i, vp]
             f.restype = i
         L.oracle_host_loop_xyp_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i]
+        L.oracle_host_loop_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i, i]
         _lib = L
     return _lib
 
@@ -85,3 +107,50 @@ def host_loop_xyp(inp: np.ndarray, w: np.ndarray, H: int, L: int, V: int, T: int
     w = np.ascontiguousarray(w, dtype=np.float64)
     lib().oracle_host_loop_xyp_f64(nx, ny, _p(inp), _p(out), _p(w), H, L, V, T, y0, ny if y1 is None else y1)
     return out
+
+
+def host_loop(inp: np.ndarray, out: np.ndarray, w: np.ndarray, H: int, L: int, V: int, T: int, cube: bool,
+              y0: int, y1: int) -> None:
+    """Plain periodic host loop over rows [y0, y1) into `out` (releases the GIL: callable from threads)."""
+    ny, nx = inp.shape
+    lib().oracle_host_loop_f64(nx, ny, _p(inp), _p(out), _p(np.ascontiguousarray(w, dtype=np.float64)), H, L, V, T,
+                               int(cube), y0, y1)
+
+
+def reference_kernels():
+    """ctypes handle on the runner of the reference's own kernels (cubin built from the reference
+    sources); None when the cubin is not present."""
+    global _refrun
+    if _refrun is None:
+        if not REF_CUBIN.exists():
+            return None
+        build()
+        R = ctypes.CDLL(str(REFRUN))
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        R.refrun_error.restype = ctypes.c_char_p
+        R.refrun_load.argtypes = [ctypes.c_char_p]
+        R.refrun_fun_ptr.argtypes = [i, ctypes.POINTER(ctypes.c_ulonglong)]
+        R.refrun_compute.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, i, ctypes.c_ulonglong]
+        if R.refrun_load(str(REF_CUBIN).encode()) != 0:
+            raise RuntimeError(R.refrun_error().decode())
+        _refrun = R
+    return _refrun
+
+
+def reference_fun_ptr(fid: int) -> int:
+    R = reference_kernels()
+    p = ctypes.c_ulonglong()
+    if R.refrun_fun_ptr(fid, ctypes.byref(p)) != 0:
+        raise RuntimeError(R.refrun_error().decode())
+    return int(p.value)
+
+
+def reference_compute(variant: int, nx: int, ny: int, num_tiles: int, bx: int, by: int, out_ptr: int, in_ptr: int,
+                      coef_ptr: int, *, num_sten: int, H: int, L: int, R: int, V: int, T: int, B: int, num_coe: int = 0,
+                      func: int = 0, halo_ptr: int | None = None) -> None:
+    """One Compute of the reference kernel itself on device buffers (device pointers)."""
+    Rr = reference_kernels()
+    rc = Rr.refrun_compute(variant, nx, ny, num_tiles, bx, by, out_ptr, in_ptr, halo_ptr or in_ptr, coef_ptr,
+                           num_sten, H, L, R, V, T, B, num_coe, func)
+    if rc != 0:
+        raise RuntimeError(Rr.refrun_error().decode())

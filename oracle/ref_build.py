@@ -1,0 +1,75 @@
+"""Builds the reference's own code from the reference sources into oracle/_ref -- TEST INFRASTRUCTURE ONLY.
+
+Nothing is copied out of the reference: the wrappers below #include the reference files where they
+lie (REF_ROOT, by default the read-only reference checkout), and only build outputs land in
+oracle/_ref (git-ignored). Where the sources are absent (e.g. on the GPU machine) nothing is built
+and the prebuilt outputs are used if they are present.
+
+Outputs:
+  custen_ref_sm103a.cubin -- the twelve cuSten kernels, unchanged, for sm_103a (oracle/ref_kernels.cu),
+                             driven by oracle/ref_runner.cpp. CUDA 13 removed one cudaMemPrefetchAsync
+                             overload the reference calls; oracle/ref_compat.h restores it.
+  libserialch.so          -- cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c compiled with gcc as the
+                             reference's compile.sh does (-O3, no contraction flags), its main renamed,
+                             with an empty hdf5.h (the header is included but unused), wrapped by
+                             oracle/ref_serial_ch.c so that its static solver functions can be called.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+REF = Path(os.environ.get("CUSTEN_REFERENCE_ROOT", "/root/reference"))
+OUT = HERE / "_ref"
+CUBIN = OUT / "custen_ref_sm103a.cubin"
+SERIAL_SO = OUT / "libserialch.so"
+
+
+def available() -> bool:
+    return (REF / "cuSten" / "src" / "kernels" / "2d_x_p_kernel.cu").exists()
+
+
+def _nvcc() -> str:
+    return shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+
+
+def build_cubin() -> Path:
+    OUT.mkdir(parents=True, exist_ok=True)
+    tmp = CUBIN.with_suffix(".cubin.tmp")
+    cmd = [_nvcc(), "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++14",
+           "-include", str(HERE / "ref_compat.h"), "-I", str(ROOT), f"-DREF_ROOT={REF}", "-o", str(tmp),
+           str(HERE / "ref_kernels.cu")]
+    subprocess.run(cmd, check=True, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    os.replace(tmp, CUBIN)
+    return CUBIN
+
+
+def build_serial_ch() -> Path:
+    OUT.mkdir(parents=True, exist_ok=True)
+    stub = OUT / "hdf5_stub"
+    stub.mkdir(exist_ok=True)
+    (stub / "hdf5.h").write_text("/* empty: serialCahnADI.c includes hdf5.h but calls nothing from it */\n")
+    tmp = SERIAL_SO.with_suffix(".so.tmp")
+    src = REF / "cuPentSpeedUp" / "serialCahnADITiming" / "serialCahnADI.c"
+    cmd = ["gcc", "-O3", "-fPIC", "-shared", "-w", "-I", str(stub), f"-DSERIAL_CH_SOURCE=\"{src}\"",
+           "-Dmain=serial_ch_main", "-o", str(tmp), str(HERE / "ref_serial_ch.c"), "-lm"]
+    subprocess.run(cmd, check=True, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    os.replace(tmp, SERIAL_SO)
+    return SERIAL_SO
+
+
+def build_if_available() -> None:
+    if not available():
+        return
+    build_cubin()
+    if (HERE / "ref_serial_ch.c").exists():
+        build_serial_ch()
+
+
+if __name__ == "__main__":
+    build_if_available()
+    print(sorted(p.name for p in OUT.glob("*")) if OUT.exists() else "reference sources not present")

@@ -51,3 +51,29 @@ void oracle_host_loop_xyp_f64(int nx, int ny, const double* in, double* out, con
         }
     }
 }
+
+/* Plain host loop with modular indexing for any variant's window (CPU baseline): periodic in both
+ * directions, out[y][x] = fma chain of w[j*H+i] * g(in[y-T+j][x-L+i]), g(c) = c (cube = 0) or
+ * c^3 - c computed as fma(c*c, c, -c) (cube = 1), rows [y0, y1). */
+void oracle_host_loop_f64(int nx, int ny, const double* in, double* out, const double* w, int H, int L, int V, int T,
+                          int cube, int y0, int y1) {
+    for (int y = y0; y < y1; ++y) {
+        for (int x = 0; x < nx; ++x) {
+            double s = 0.0;
+            int k = 0;
+            for (int j = 0; j < V; ++j) {
+                int yy = y - T + j;
+                yy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
+                const double* row = in + (size_t)yy * nx;
+                for (int i = 0; i < H; ++i) {
+                    int xx = x - L + i;
+                    xx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
+                    double c = row[xx];
+                    double g = cube ? fma(c * c, c, -c) : c;
+                    s = fma(w[k++], g, s);
+                }
+            }
+            out[(size_t)y * nx + x] = s;
+        }
+    }
+}
