@@ -49,6 +49,8 @@ def lib() -> ctypes.CDLL:
         vp, i, ull, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_size_t
         L.custen_last_error.restype = ctypes.c_char_p
         L.custen_kernel_launches.restype = ull
+        L.custen_kernel_launches_tma.restype = ull
+        L.custen_device_error.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
         L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
         L.custen_compute.argtypes = [vp, i]
         L.custen_compute_on_stream.argtypes = [vp, i, vp]
@@ -105,6 +107,17 @@ def probe_fma_rate(dtype: int = F64) -> float:
 
 def kernel_launches() -> int:
     return int(lib().custen_kernel_launches())
+
+
+def kernel_launches_tma() -> int:
+    return int(lib().custen_kernel_launches_tma())
+
+
+def device_error(clear: bool = True) -> int:
+    """Device-side error flags (bit 0: a bounded mbarrier wait expired)."""
+    f = ctypes.c_uint()
+    _check(lib().custen_device_error(ctypes.byref(f), int(clear)))
+    return int(f.value)
 
 
 class Stencil:

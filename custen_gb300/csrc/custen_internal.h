@@ -127,7 +127,8 @@ struct StreamBlock {
 constexpr uint32_t kPlanMagic = 0xC5E7B300u;
 
 // Launch entry points implemented in the kernel translation units.
-cudaError_t launch_stencil_f64(const StencilArgs& a, cudaStream_t s);
-cudaError_t launch_stencil_f32(const StencilArgs& a, cudaStream_t s);
+// *path is set to 1 when the TMA-staged kernel ran, 0 for the plain-load kernel.
+cudaError_t launch_stencil_f64(const StencilArgs& a, cudaStream_t s, int* path);
+cudaError_t launch_stencil_f32(const StencilArgs& a, cudaStream_t s, int* path);
 
 }  // namespace custen

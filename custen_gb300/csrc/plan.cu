@@ -27,8 +27,12 @@ static_assert(offsetof(cuSten_t, devFunc) == 192, "cuSten_t::devFunc offset");
 
 namespace custen {
 
+// Device-side error word: bit 0 = an mbarrier wait of a TMA-staged kernel expired.
+__device__ unsigned int g_custen_device_error = 0;
+
 static thread_local std::string g_last_error;
 static std::atomic<unsigned long long> g_launches{0};
+static std::atomic<unsigned long long> g_launches_tma{0};
 
 enum { ST_OK = 0, ST_CUDA = 1, ST_ARG = 2, ST_UNSUPPORTED = 3 };
 
@@ -281,10 +285,12 @@ static cudaError_t prefetch(const void* p, size_t bytes, int dev, cudaStream_t s
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 static cudaError_t launch(const StencilArgs& a, int dtype, cudaStream_t s, PlanPrivate* p) {
-    cudaError_t e = dtype == DT_F64 ? launch_stencil_f64(a, s) : launch_stencil_f32(a, s);
+    int path = 0;
+    cudaError_t e = dtype == DT_F64 ? launch_stencil_f64(a, s, &path) : launch_stencil_f32(a, s, &path);
     if (e == cudaSuccess) {
         ++p->launches;
         g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (path == 1) g_launches_tma.fetch_add(1, std::memory_order_relaxed);
     }
     return e;
 }
@@ -517,6 +523,7 @@ int custen_abi_version(void) { return 1; }
 int custen_sizeof_handle(void) { return (int)sizeof(cuSten_t); }
 const char* custen_last_error(void) { return g_last_error.c_str(); }
 unsigned long long custen_kernel_launches(void) { return g_launches.load(); }
+unsigned long long custen_kernel_launches_tma(void) { return g_launches_tma.load(); }
 
 int custen_create(cuSten_t* h, int variant, int dtype, int dev, int nt, int nx, int ny, int bx, int by, void* out,
                   void* in, void* coef, int H, int L, int R, int V, int T, int B, int ncoef, void* func) {
@@ -606,6 +613,16 @@ int custen_create_2d_xynp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int 
                               double* in, double* coe, int Hs, int L, int R, int Vs, int T, int B, double* func) {
     return create_plan(h, V_XYNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, Hs, L, R, Vs, T, B, Hs * Vs,
                        func, Hs * Vs);
+}
+
+int custen_device_error(unsigned int* flags, int clear) {
+    if (flags == nullptr) return fail_arg("flags pointer is NULL");
+    CU_TRY(cudaMemcpyFromSymbol(flags, g_custen_device_error, sizeof(unsigned int)), "Reading device error flags");
+    if (clear) {
+        unsigned int z = 0;
+        CU_TRY(cudaMemcpyToSymbol(g_custen_device_error, &z, sizeof(z)), "Clearing device error flags");
+    }
+    return ST_OK;
 }
 
 int custen_malloc_managed(void** ptr, size_t bytes) {

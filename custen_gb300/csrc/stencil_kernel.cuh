@@ -125,6 +125,26 @@ __device__ __forceinline__ void stage_tile_ldg(const StencilArgs& a, T* tile, co
     }
 }
 
+// True when every point of the tile is written with its stencil value (no write rule applies).
+__device__ __forceinline__ bool tile_all_write(const StencilArgs& a, int x0, int x1, int gy0, int gy1) {
+    switch (a.variant) {
+    case V_XNP:
+    case V_XNPFUN:
+        return x0 >= a.L && x1 <= a.nx - a.R;
+    case V_YNP:
+    case V_YNPFUN:
+        return gy0 >= a.T && gy1 <= a.nyTile * a.numTiles - a.B;
+    case V_XYNP:
+    case V_XYNPFUN: {
+        if (x0 < a.bx || x1 > a.nx - a.bx) return false;
+        const int ny = a.nyTile * a.numTiles;
+        return gy0 >= a.by && gy1 <= ny - a.by;
+    }
+    default:
+        return true;
+    }
+}
+
 template <typename T> using FunX = T (*)(T*, T*, int);
 template <typename T> using FunY = T (*)(T*, T*, int, int);
 template <typename T> using FunXY = T (*)(T*, T*, int, int, int, int);
@@ -133,7 +153,7 @@ template <typename T> using FunXY = T (*)(T*, T*, int, int, int, int);
 template <typename T, int TW, int TH, int RPT>
 __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile, T* coef_s, const int* list_off,
                                                   const T* list_w, int nlist, const TileGeom<T, TW, TH>& g,
-                                                  int x0, int y0, int tx, int ty, bool is_fun) {
+                                                  int x0, int y0, int tx, int ty, bool is_fun, bool all_write_tile) {
     constexpr int VEC = VecT<T>::n;
     using V = typename VecT<T>::type;
     const int c0 = tx * VEC;    // tile-local column of the first output
@@ -182,12 +202,17 @@ __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile,
         T* orow = reinterpret_cast<T*>(a.out) + (size_t)gyl * a.nx;
         int act[VEC];
         bool all_write = true;
+        if (all_write_tile && gx + VEC <= a.nx) {
 #pragma unroll
-        for (int v = 0; v < VEC; ++v) {
-            act[v] = (gx + v < a.nx) ? point_action(a.variant, gx + v, gy, a.nx, a.L, a.R, a.T, a.B, a.bx, a.by,
-                                                    a.nyTile, a.numTiles)
-                                     : ACT_SKIP;
-            all_write = all_write && (act[v] == ACT_WRITE);
+            for (int v = 0; v < VEC; ++v) act[v] = ACT_WRITE;
+        } else {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                act[v] = (gx + v < a.nx) ? point_action(a.variant, gx + v, gy, a.nx, a.L, a.R, a.T, a.B, a.bx,
+                                                        a.by, a.nyTile, a.numTiles)
+                                         : ACT_SKIP;
+                all_write = all_write && (act[v] == ACT_WRITE);
+            }
         }
         if (all_write && a.vec_ok) {
             V outv;

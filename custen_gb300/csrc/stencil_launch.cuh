@@ -1,6 +1,11 @@
 // Kernel entry and launcher template for the shared-memory tiled stencil (see stencil_kernel.cuh).
 #pragma once
 
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+
 #include "stencil_kernel.cuh"
 #include "stencil_tma.cuh"
 
@@ -13,7 +18,7 @@ stencil_ldg_kernel(const __grid_constant__ StencilArgs a) {
     constexpr int VEC = VecT<T>::n;
     constexpr int NTX = TW / VEC;
     constexpr int NT = NTX * (TH / RPT);
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(16) unsigned char smem[];
     TileGeom<T, TW, TH> g(a);
     T* tile = reinterpret_cast<T*>(smem);
     T* coef_s = reinterpret_cast<T*>(smem + g.coef_off(a));
@@ -24,8 +29,9 @@ stencil_ldg_kernel(const __grid_constant__ StencilArgs a) {
     const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
     stage_tile_ldg<T, TW, TH, NT>(a, tile, g, x0, y0, tid);
     const int nlist = stage_coefficients<T, NT>(a, coef_s, list_off, list_w, g.SW, tid, is_fun);  // syncs
+    const bool all_write = tile_all_write(a, x0, x0 + TW, a.row0 + y0, a.row0 + y0 + TH);
     compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
-                                      threadIdx.y, is_fun);
+                                      threadIdx.y, is_fun, all_write);
 }
 
 // Largest dynamic shared memory a block may opt in to on the current device.
@@ -57,6 +63,79 @@ cudaError_t launch_ldg(const StencilArgs& a, cudaStream_t s) {
     dim3 block(TW / VEC, TH / RPT);
     dim3 grid((a.nx + TW - 1) / TW, (a.rows + TH - 1) / TH);
     stencil_ldg_kernel<T, TW, TH, RPT><<<grid, block, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link-time libcuda dependency).
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+template <typename T>
+inline bool encode_rows_map(CUtensorMap* m, const void* base, int nx, int rows, int box_w, int box_h) {
+    auto enc = tensor_map_encoder();
+    if (!enc || base == nullptr || rows < 1 || box_h < 1) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)nx * sizeof(T)};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(m, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                     const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+inline int sm_count() {
+    static int cached[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    if (dev >= 0 && dev < 64) cached[dev] = v;
+    return v;
+}
+
+// TMA path: returns cudaErrorNotSupported (without launching) when the geometry does not allow it.
+template <typename T, int TW, int TH, int RPT, int S>
+cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
+    constexpr int VEC = VecT<T>::n;
+    TileGeom<T, TW, TH> g(a);
+    // One box per window: at most 256 columns and 256 rows; rows and columns tile exactly; rows
+    // 16-byte aligned (global address and stride rules of cuTensorMapEncodeTiled).
+    if (!a.vec_ok || a.nx % TW != 0 || a.rows % TH != 0 || g.SW > 256 || g.SR > 256) return cudaErrorNotSupported;
+    TmaMaps maps;
+    memset(&maps, 0, sizeof(maps));
+    if (!encode_rows_map<T>(&maps.win, a.in, a.nx, a.rows, g.SW, g.SR)) return cudaErrorNotSupported;
+    const size_t stage_bytes = round_up_int((int)((size_t)g.SR * g.SW * sizeof(T)), 128);
+    const size_t smem = S * stage_bytes + round_up_int(a.ncoef * (int)sizeof(T), 16) +
+                        round_up_int(a.ncoef * (int)sizeof(int), 16) + round_up_int(a.ncoef * (int)sizeof(T), 16) +
+                        256;   // 128 bytes of alignment slack for the ring base + tail padding
+    auto kern = stencil_tma_kernel<T, TW, TH, RPT, S>;
+    cudaError_t e = ensure_smem(kern, smem);
+    if (e != cudaSuccess) return e == cudaErrorInvalidConfiguration ? cudaErrorNotSupported : e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (TW / VEC) * (TH / RPT), smem);
+    if (e != cudaSuccess || per_sm < 1) return cudaErrorNotSupported;
+    const int tiles_x = a.nx / TW;
+    const int tiles_total = tiles_x * (a.rows / TH);
+    const int grid = std::min(tiles_total, per_sm * sm_count());
+    dim3 block(TW / VEC, TH / RPT);
+    kern<<<grid, block, smem, s>>>(maps, a, tiles_x, tiles_total);
     return cudaGetLastError();
 }
 

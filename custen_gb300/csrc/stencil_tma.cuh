@@ -1,2 +1,207 @@
-// TMA staging path of the stencil kernel (filled in once the plain-load path is parity-checked).
+// TMA-staged, persistent, multi-stage stencil kernel (sm_103a).
+//
+// Each CTA walks the output tiles tile = blockIdx.x + k * gridDim.x and keeps S tile windows in
+// flight in a shared-memory ring. One thread issues one tensor-memory-accelerator copy per window: a
+// box of SW = LP + TW + RP columns by SR = T + TH + B rows starting at (x0 - LP, y0 - T), landing at a
+// 128-byte aligned stage. Completion is signalled on the stage's mbarrier (complete_tx); the next
+// tiles' copies run while the current tile computes. Rows and columns outside the launch arrive
+// zero-filled; edge tiles then fetch their halo rows through the halo pointers and their wrapped
+// columns (periodic variants) with plain loads -- two tile rows and two tile columns of the field.
+//
+// Every mbarrier wait is bounded: on expiry the CTA records an error in g_custen_device_error, waits
+// (bounded) for its own copies still in flight, and returns.
 #pragma once
+
+#include <cuda.h>
+
+#include "stencil_kernel.cuh"
+
+namespace custen {
+
+extern __device__ unsigned int g_custen_device_error;
+constexpr unsigned int kErrMbarrierTimeout = 1u;
+constexpr long long kWaitLimit = 1ll << 22;   // try_wait rounds (each may suspend ~µs) before giving up
+
+struct TmaMaps {
+    CUtensorMap win;   // launch rows, box {SW, SR}
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait for the phase with the given parity to complete; false on expiry.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t addr = smem_u32(bar);
+    for (long long i = 0; i < kWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Issue the copy of one tile window into the (128-byte aligned) stage `dst`.
+template <typename T, int TW, int TH>
+__device__ __forceinline__ void issue_window(const StencilArgs& a, const TmaMaps& m, T* dst, uint64_t* bar, int x0,
+                                             int y0, const TileGeom<T, TW, TH>& g) {
+    mbar_arrive_expect_tx(bar, (uint32_t)(g.SR * g.SW * sizeof(T)));
+    tma_load_2d(dst, &m.win, x0 - g.LP, y0 - a.T, bar);
+}
+
+// Edge tiles: replace the zero-filled cells outside the launch. Rows above / below the launch come
+// through the halo pointers (when the variant reads them); columns outside [0, nx) wrap around
+// (periodic variants). Cells with no source are left as zeros: no written point reads them.
+template <typename T, int TW, int TH, int NT>
+__device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const TileGeom<T, TW, TH>& g, int x0, int y0,
+                                           int tid, bool rows_fix, bool cols_fix) {
+    if (rows_fix) {
+        // whole halo rows (all SW columns) of the rows outside [0, rows)
+        const int total = g.SR * g.SW;
+        for (int e = tid; e < total; e += NT) {
+            const int r = e / g.SW;
+            const int gyl = y0 - a.T + r;
+            if (gyl >= 0 && gyl < a.rows) continue;
+            const T* rowp = launch_row<T>(a, gyl);
+            if (rowp == nullptr) continue;
+            const int c = e - r * g.SW;
+            int x = x0 - g.LP + c;
+            if (x < 0 || x >= a.nx) {
+                if (!a.wrap_x) continue;
+                x = x < 0 ? x + a.nx : x - a.nx;
+                if (x < 0 || x >= a.nx) continue;
+            }
+            tile[e] = __ldg(rowp + x);
+        }
+    }
+    if (cols_fix) {
+        // wrapped halo columns of the rows inside the launch
+        const int ncols = g.LP + g.RP;
+        const int total = g.SR * ncols;
+        for (int e = tid; e < total; e += NT) {
+            const int r = e / ncols;
+            const int gyl = y0 - a.T + r;
+            if (gyl < 0 || gyl >= a.rows) continue;
+            const int k = e - r * ncols;
+            const int c = (k < g.LP) ? k : (g.LP + TW + (k - g.LP));
+            const int x = x0 - g.LP + c;
+            if (x >= 0 && x < a.nx) continue;
+            const int xw = x < 0 ? x + a.nx : x - a.nx;
+            if (xw < 0 || xw >= a.nx) continue;
+            tile[r * g.SW + c] = __ldg(reinterpret_cast<const T*>(a.in) + (size_t)gyl * a.nx + xw);
+        }
+    }
+}
+
+template <typename T, int TW, int TH, int RPT, int S>
+__global__ void __launch_bounds__((TW / VecT<T>::n) * (TH / RPT))
+stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__ StencilArgs a, int tiles_x,
+                   int tiles_total) {
+    constexpr int VEC = VecT<T>::n;
+    constexpr int NTX = TW / VEC;
+    constexpr int NT = NTX * (TH / RPT);
+    // The dynamic segment is only guaranteed 16-byte alignment (with relocatable device code its
+    // placement after the static shared objects is fixed at link time); the ring is aligned to 128
+    // bytes at run time inside 128 bytes of slack. The address goes through an empty asm so that no
+    // alignment assumption can fold the computation away.
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[S];
+    TileGeom<T, TW, TH> g(a);
+    const size_t stage_elems = (size_t)g.SR * g.SW;
+    const size_t stage_bytes = round_up_int((int)(stage_elems * sizeof(T)), 128);
+    uint32_t raw_addr = smem_u32(smem_raw);
+    asm volatile("" : "+r"(raw_addr));
+    unsigned char* smem = smem_raw + ((128u - (raw_addr & 127u)) & 127u);
+    T* ring = reinterpret_cast<T*>(smem);
+    unsigned char* after = smem + S * stage_bytes;
+    T* coef_s = reinterpret_cast<T*>(after);
+    int* list_off = reinterpret_cast<int*>(after + round_up_int(a.ncoef * (int)sizeof(T), 16));
+    T* list_w = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(list_off) +
+                                     round_up_int(a.ncoef * (int)sizeof(int), 16));
+    const int tid = threadIdx.x + threadIdx.y * NTX;
+    const bool is_fun = variant_is_fun(a.variant);
+
+    if (tid == 0) {
+        for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int k = 0; k < S; ++k) {
+            const int t = blockIdx.x + k * gridDim.x;
+            if (t >= tiles_total) break;
+            const int tyi = t / tiles_x, txi = t - tyi * tiles_x;
+            issue_window<T, TW, TH>(a, maps, ring + (size_t)k * stage_bytes / sizeof(T), &full[k], txi * TW,
+                                    tyi * TH, g);
+        }
+    }
+    const int nlist = stage_coefficients<T, NT>(a, coef_s, list_off, list_w, g.SW, tid, is_fun);  // syncs
+
+    for (int it = 0;; ++it) {
+        const int t = blockIdx.x + it * gridDim.x;
+        if (t >= tiles_total) break;
+        const int s = it % S;
+        const uint32_t parity = (uint32_t)((it / S) & 1);
+        T* tile = ring + (size_t)s * stage_bytes / sizeof(T);
+        const bool ok = mbar_wait(&full[s], parity);
+        if (__syncthreads_or(!ok)) {
+            // A copy never completed: record it, wait (bounded) for the copies this CTA still has in
+            // flight, and leave.
+            if (tid == 0) {
+                atomicOr(&g_custen_device_error, kErrMbarrierTimeout);
+                for (int k = 0; k < S; ++k) {
+                    const int tk = blockIdx.x + (it + k) * gridDim.x;
+                    if (tk >= tiles_total) break;
+                    mbar_wait(&full[(it + k) % S], (uint32_t)(((it + k) / S) & 1));
+                }
+            }
+            __syncthreads();
+            return;
+        }
+        const int tyi = t / tiles_x, txi = t - tyi * tiles_x;
+        const int x0 = txi * TW, y0 = tyi * TH;
+        const bool rows_fix = (y0 == 0 && a.T > 0 && a.has_top) || (y0 + TH == a.rows && a.B > 0 && a.has_bot);
+        const bool cols_fix = a.wrap_x && (x0 == 0 || x0 + TW == a.nx) && (a.L > 0 || a.R > 0);
+        if (rows_fix || cols_fix) {
+            edge_fixup<T, TW, TH, NT>(a, tile, g, x0, y0, tid, rows_fix, cols_fix);
+            __syncthreads();
+        }
+        const bool all_write = tile_all_write(a, x0, x0 + TW, a.row0 + y0, a.row0 + y0 + TH);
+        compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
+                                          threadIdx.y, is_fun, all_write);
+        fence_proxy_async_smem();
+        __syncthreads();   // every thread is done with stage s
+        if (tid == 0) {
+            const int tn = t + S * gridDim.x;
+            if (tn < tiles_total) {
+                const int tyn = tn / tiles_x, txn = tn - tyn * tiles_x;
+                issue_window<T, TW, TH>(a, maps, tile, &full[s], txn * TW, tyn * TH, g);
+            }
+        }
+    }
+}
+
+}  // namespace custen

@@ -36,6 +36,7 @@ int custen_abi_version(void);                 /* increments when an entry point 
 int custen_sizeof_handle(void);               /* sizeof(cuSten_t): 200 on LP64 */
 const char* custen_last_error(void);
 unsigned long long custen_kernel_launches(void);   /* kernels launched by this library so far */
+unsigned long long custen_kernel_launches_tma(void);   /* of which used the TMA-staged stencil kernel */
 
 /* ---- handle life cycle: generic form ----
  * H/L/R: window width and extents in x; V/T/B in y. X variants: V=1, T=B=0; Y variants: H=1, L=R=0.
@@ -117,6 +118,11 @@ int custen_builtin_function(int id, int dtype, void** func);
  * Sustained FMA rate of this GPU (FMA per second, 8 independent chains per thread, all SMs), the
  * compute-roofline denominator of the FP64 stencils. No counterpart in the reference. */
 int custen_probe_fma_rate(int dtype, double* fma_per_s);
+
+/* Device-side error flags raised by kernels instead of trapping (bit 0: a bounded mbarrier wait of a
+ * TMA-staged kernel expired; the kernel then returned early). Synchronous; clear != 0 resets them.
+ * No counterpart in the reference (its kernels have no waits). */
+int custen_device_error(unsigned int* flags, int clear);
 
 /* ---- memory helpers for hosts without a CUDA runtime binding ---- */
 int custen_malloc_managed(void** ptr, size_t bytes);

@@ -197,3 +197,32 @@ def test_weights_reread_every_compute(gpu):
     ref = np.zeros_like(inp)
     oracle.stencil(cs.XP, ref, inp, w2, num_tiles=1, block_x=32, block_y=8, H=3, L=1, R=1, V=1, T=0, B=0)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=cs.VARIANT_NAMES)
+@pytest.mark.parametrize("tiles", [1, 2, 4])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_parity_tma_path(gpu, variant, tiles, dtype):
+    """Geometries the TMA-staged persistent kernel takes (rows tile by 32, columns by 64 / 128 elements,
+    16-byte aligned rows): bit-exact, and the TMA kernel is the one that ran."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    fun = variant in (cs.XPFUN, cs.XNPFUN, cs.YPFUN, cs.YNPFUN, cs.XYPFUN, cs.XYNPFUN)
+    geom = geometry(variant, "asym" if not fun else "sym")
+    fun_id = FUN_IDS[d][1] if fun else -1
+    before = cs.kernel_launches_tma()
+    got, ref, st, pre = run_both(variant, 256, 128, tiles, 32, 8, geom, dtype=dtype, fun_id=fun_id,
+                                 seed=variant + 40 * tiles)
+    assert cs.kernel_launches_tma() > before, "the TMA-staged kernel did not run"
+    check(got, ref, st, pre)
+    assert cs.device_error() == 0
+
+
+@pytest.mark.parametrize("variant", [cs.XP, cs.YP, cs.XYP, cs.XYNP])
+def test_tma_path_periodic_edges_wide_halo(gpu, variant):
+    """Halo wider than one 16-byte vector (L = R = T = B = 3): periodic edge tiles take the wrap fix-up."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    geom = {0: (7, 3, 3, 1, 0, 0), 1: (1, 0, 0, 7, 3, 3), 2: (7, 3, 3, 7, 3, 3)}[d]
+    before = cs.kernel_launches_tma()
+    got, ref, st, pre = run_both(variant, 192, 96, 3, 32, 8, geom, seed=77)
+    assert cs.kernel_launches_tma() > before
+    check(got, ref, st, pre)
