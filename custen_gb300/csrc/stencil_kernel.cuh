@@ -149,6 +149,49 @@ template <typename T> using FunX = T (*)(T*, T*, int);
 template <typename T> using FunY = T (*)(T*, T*, int, int);
 template <typename T> using FunXY = T (*)(T*, T*, int, int, int, int);
 
+// Store VEC x RPT outputs of one thread: 16-byte vector stores where every point is written with its
+// stencil value, the reference's write rules (untouched / zero) elsewhere.
+template <typename T, int RPT>
+__device__ __forceinline__ void store_outputs(const StencilArgs& a, const T (&acc)[RPT][VecT<T>::n], int gx, int gy0,
+                                              bool all_write_tile) {
+    constexpr int VEC = VecT<T>::n;
+    using V = typename VecT<T>::type;
+#pragma unroll
+    for (int rr = 0; rr < RPT; ++rr) {
+        const int gyl = gy0 + rr;
+        if (gyl >= a.rows) break;
+        const int gy = a.row0 + gyl;
+        T* orow = reinterpret_cast<T*>(a.out) + (size_t)gyl * a.nx;
+        int act[VEC];
+        bool all_write = true;
+        if (all_write_tile && gx + VEC <= a.nx) {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) act[v] = ACT_WRITE;
+        } else {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                act[v] = (gx + v < a.nx) ? point_action(a.variant, gx + v, gy, a.nx, a.L, a.R, a.T, a.B, a.bx,
+                                                        a.by, a.nyTile, a.numTiles)
+                                         : ACT_SKIP;
+                all_write = all_write && (act[v] == ACT_WRITE);
+            }
+        }
+        if (all_write && a.vec_ok) {
+            V outv;
+            T* o = reinterpret_cast<T*>(&outv);
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) o[v] = acc[rr][v];
+            *reinterpret_cast<V*>(orow + gx) = outv;
+        } else {
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) {
+                if (act[v] == ACT_WRITE) orow[gx + v] = acc[rr][v];
+                else if (act[v] == ACT_ZERO) orow[gx + v] = T(0);
+            }
+        }
+    }
+}
+
 // Compute VEC x RPT outputs per thread from the staged window and store them.
 template <typename T, int TW, int TH, int RPT>
 __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile, T* coef_s, const int* list_off,
@@ -193,41 +236,81 @@ __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile,
         }
     }
 
-    const int gx = x0 + c0;
+    store_outputs<T, RPT>(a, acc, x0 + c0, y0 + r0, all_write_tile);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Compile-time stencil shapes: register sliding window along y, 16-byte conflict-free shared loads.
+// ---------------------------------------------------------------------------------------------
+template <int H_, int L_, int V_, int T_>
+struct Shape {
+    static constexpr int H = H_, L = L_, V = V_, T = T_;
+};
+
+// Kernel modes: 0 generic (list of non-zero weights), 1 device function, >= 2 the shapes below.
+enum : int { MODE_LIST = 0, MODE_FUN = 1, MODE_FIRST_SHAPE = 2, MODE_COUNT = 10 };
+template <int MODE> struct ShapeOf { using type = Shape<1, 0, 1, 0>; };
+template <> struct ShapeOf<2> { using type = Shape<3, 1, 1, 0>; };   // X 3-point
+template <> struct ShapeOf<3> { using type = Shape<5, 2, 1, 0>; };   // X 5-point
+template <> struct ShapeOf<4> { using type = Shape<9, 4, 1, 0>; };   // X 9-point
+template <> struct ShapeOf<5> { using type = Shape<1, 0, 3, 1>; };   // Y 3-point
+template <> struct ShapeOf<6> { using type = Shape<1, 0, 5, 2>; };   // Y 5-point
+template <> struct ShapeOf<7> { using type = Shape<1, 0, 9, 4>; };   // Y 9-point
+template <> struct ShapeOf<8> { using type = Shape<3, 1, 3, 1>; };   // XY 3 x 3
+template <> struct ShapeOf<9> { using type = Shape<5, 2, 5, 2>; };   // XY 5 x 5
+
+// Host: the shape mode matching a launch's window, or MODE_LIST.
+inline int shape_mode(int H, int L, int V, int T) {
+    const int tab[8][4] = {{3, 1, 1, 0}, {5, 2, 1, 0}, {9, 4, 1, 0}, {1, 0, 3, 1},
+                           {1, 0, 5, 2}, {1, 0, 9, 4}, {3, 1, 3, 1}, {5, 2, 5, 2}};
+    for (int k = 0; k < 8; ++k)
+        if (tab[k][0] == H && tab[k][1] == L && tab[k][2] == V && tab[k][3] == T) return MODE_FIRST_SHAPE + k;
+    return MODE_LIST;
+}
+
+// Each thread slides down its RPT output rows: input row r0 + k is read once (NV 16-byte loads covering
+// the columns its VEC outputs need) and applied to every output row whose window contains it. Per
+// output the FMAs run j = 0..V-1 (rows, top first), i = 0..H-1 -- the reference order
+// (2d_xy_p_kernel.cu:507-520) -- all weights included, zeros too.
+template <typename T, int TW, int TH, int RPT, class SH>
+__device__ __forceinline__ void compute_window_store(const StencilArgs& a, const T* tile, const T* coef_s,
+                                                     const TileGeom<T, TW, TH>& g, int x0, int y0, int tx, int ty,
+                                                     bool all_write_tile) {
+    constexpr int VEC = VecT<T>::n;
+    using VV = typename VecT<T>::type;
+    constexpr int LP = round_up_int(SH::L, VEC);
+    constexpr int D = LP - SH::L;                       // first needed column inside the aligned segment
+    constexpr int NV = (D + VEC + SH::H - 1 + VEC - 1) / VEC;
+    const int c0 = tx * VEC, r0 = ty * RPT;
+    T acc[RPT][VEC];
 #pragma unroll
-    for (int rr = 0; rr < RPT; ++rr) {
-        const int gyl = y0 + r0 + rr;
-        if (gyl >= a.rows) break;
-        const int gy = a.row0 + gyl;
-        T* orow = reinterpret_cast<T*>(a.out) + (size_t)gyl * a.nx;
-        int act[VEC];
-        bool all_write = true;
-        if (all_write_tile && gx + VEC <= a.nx) {
+    for (int rr = 0; rr < RPT; ++rr)
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) act[v] = ACT_WRITE;
-        } else {
+        for (int v = 0; v < VEC; ++v) acc[rr][v] = T(0);
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) {
-                act[v] = (gx + v < a.nx) ? point_action(a.variant, gx + v, gy, a.nx, a.L, a.R, a.T, a.B, a.bx,
-                                                        a.by, a.nyTile, a.numTiles)
-                                         : ACT_SKIP;
-                all_write = all_write && (act[v] == ACT_WRITE);
-            }
+    for (int k = 0; k < RPT + SH::V - 1; ++k) {
+        T seg[NV * VEC];
+        const VV* src = reinterpret_cast<const VV*>(tile + (r0 + k) * g.SW + c0);
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const VV t = src[q];
+            const T* tp = reinterpret_cast<const T*>(&t);
+#pragma unroll
+            for (int v = 0; v < VEC; ++v) seg[q * VEC + v] = tp[v];
         }
-        if (all_write && a.vec_ok) {
-            V outv;
-            T* o = reinterpret_cast<T*>(&outv);
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) o[v] = acc[rr][v];
-            *reinterpret_cast<V*>(orow + gx) = outv;
-        } else {
+        for (int rr = 0; rr < RPT; ++rr) {
+            const int j = k - rr;
+            if (j < 0 || j >= SH::V) continue;
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) {
-                if (act[v] == ACT_WRITE) orow[gx + v] = acc[rr][v];
-                else if (act[v] == ACT_ZERO) orow[gx + v] = T(0);
+            for (int i = 0; i < SH::H; ++i) {
+                const T w = coef_s[j * SH::H + i];
+#pragma unroll
+                for (int v = 0; v < VEC; ++v) acc[rr][v] = fma(w, seg[D + v + i], acc[rr][v]);
             }
         }
     }
+    store_outputs<T, RPT>(a, acc, x0 + c0, y0 + r0, all_write_tile);
 }
 
 }  // namespace custen

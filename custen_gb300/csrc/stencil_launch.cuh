@@ -111,8 +111,8 @@ inline int sm_count() {
 }
 
 // TMA path: returns cudaErrorNotSupported (without launching) when the geometry does not allow it.
-template <typename T, int TW, int TH, int RPT, int S>
-cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
+template <typename T, int TW, int TH, int RPT, int S, int MODE>
+cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
     constexpr int VEC = VecT<T>::n;
     TileGeom<T, TW, TH> g(a);
     // One box per window: at most 256 columns and 256 rows; rows and columns tile exactly; rows
@@ -125,7 +125,7 @@ cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
     const size_t smem = S * stage_bytes + round_up_int(a.ncoef * (int)sizeof(T), 16) +
                         round_up_int(a.ncoef * (int)sizeof(int), 16) + round_up_int(a.ncoef * (int)sizeof(T), 16) +
                         256;   // 128 bytes of alignment slack for the ring base + tail padding
-    auto kern = stencil_tma_kernel<T, TW, TH, RPT, S>;
+    auto kern = stencil_tma_kernel<T, TW, TH, RPT, S, MODE>;
     cudaError_t e = ensure_smem(kern, smem);
     if (e != cudaSuccess) return e == cudaErrorInvalidConfiguration ? cudaErrorNotSupported : e;
     int per_sm = 0;
@@ -137,6 +137,23 @@ cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
     dim3 block(TW / VEC, TH / RPT);
     kern<<<grid, block, smem, s>>>(maps, a, tiles_x, tiles_total);
     return cudaGetLastError();
+}
+
+template <typename T, int TW, int TH, int RPT, int S>
+cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
+    const int mode = variant_is_fun(a.variant) ? (int)MODE_FUN : shape_mode(a.H, a.L, a.V, a.T);
+    switch (mode) {
+    case MODE_FUN: return launch_tma_mode<T, TW, TH, RPT, S, MODE_FUN>(a, s);
+    case 2: return launch_tma_mode<T, TW, TH, RPT, S, 2>(a, s);
+    case 3: return launch_tma_mode<T, TW, TH, RPT, S, 3>(a, s);
+    case 4: return launch_tma_mode<T, TW, TH, RPT, S, 4>(a, s);
+    case 5: return launch_tma_mode<T, TW, TH, RPT, S, 5>(a, s);
+    case 6: return launch_tma_mode<T, TW, TH, RPT, S, 6>(a, s);
+    case 7: return launch_tma_mode<T, TW, TH, RPT, S, 7>(a, s);
+    case 8: return launch_tma_mode<T, TW, TH, RPT, S, 8>(a, s);
+    case 9: return launch_tma_mode<T, TW, TH, RPT, S, 9>(a, s);
+    default: return launch_tma_mode<T, TW, TH, RPT, S, MODE_LIST>(a, s);
+    }
 }
 
 }  // namespace custen

@@ -119,8 +119,11 @@ __device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const 
     }
 }
 
-template <typename T, int TW, int TH, int RPT, int S>
-__global__ void __launch_bounds__((TW / VecT<T>::n) * (TH / RPT))
+// MODE: MODE_LIST (weights, generic window), MODE_FUN (device function), or a compile-time shape.
+// FP64 shape kernels fall back to the list when a weight is zero (FP64 FMAs are the bottleneck on
+// GB300; dropping exact zeros is bit-neutral for finite inputs).
+template <typename T, int TW, int TH, int RPT, int S, int MODE>
+__global__ void __launch_bounds__((TW / VecT<T>::n) * (TH / RPT), MODE == MODE_FUN ? 2 : 3)
 stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__ StencilArgs a, int tiles_x,
                    int tiles_total) {
     constexpr int VEC = VecT<T>::n;
@@ -145,7 +148,7 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
     T* list_w = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(list_off) +
                                      round_up_int(a.ncoef * (int)sizeof(int), 16));
     const int tid = threadIdx.x + threadIdx.y * NTX;
-    const bool is_fun = variant_is_fun(a.variant);
+    constexpr bool is_fun = (MODE == MODE_FUN);
 
     if (tid == 0) {
         for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
@@ -190,8 +193,18 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
             __syncthreads();
         }
         const bool all_write = tile_all_write(a, x0, x0 + TW, a.row0 + y0, a.row0 + y0 + TH);
-        compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
-                                          threadIdx.y, is_fun, all_write);
+        if constexpr (MODE >= MODE_FIRST_SHAPE) {
+            using SH = typename ShapeOf<MODE>::type;
+            if (sizeof(T) == 4 || nlist == SH::H * SH::V)
+                compute_window_store<T, TW, TH, RPT, SH>(a, tile, coef_s, g, x0, y0, threadIdx.x, threadIdx.y,
+                                                         all_write);
+            else
+                compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0,
+                                                  threadIdx.x, threadIdx.y, false, all_write);
+        } else {
+            compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
+                                              threadIdx.y, is_fun, all_write);
+        }
         fence_proxy_async_smem();
         __syncthreads();   // every thread is done with stage s
         if (tid == 0) {

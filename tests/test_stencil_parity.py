@@ -226,3 +226,37 @@ def test_tma_path_periodic_edges_wide_halo(gpu, variant):
     got, ref, st, pre = run_both(variant, 192, 96, 3, 32, 8, geom, seed=77)
     assert cs.kernel_launches_tma() > before
     check(got, ref, st, pre)
+
+
+SHAPES = {  # the compile-time register-window shapes: (variant, H, L, R, V, T, B)
+    "X3": (cs.XP, 3, 1, 1, 1, 0, 0), "X5": (cs.XNP, 5, 2, 2, 1, 0, 0), "X9": (cs.XP, 9, 4, 4, 1, 0, 0),
+    "Y3": (cs.YNP, 1, 0, 0, 3, 1, 1), "Y5": (cs.YP, 1, 0, 0, 5, 2, 2), "Y9": (cs.YP, 1, 0, 0, 9, 4, 4),
+    "XY3": (cs.XYP, 3, 1, 1, 3, 1, 1), "XY5": (cs.XYNP, 5, 2, 2, 5, 2, 2),
+}
+
+
+@pytest.mark.parametrize("shape", list(SHAPES))
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+@pytest.mark.parametrize("dense", [True, False], ids=["dense", "zeros"])
+def test_parity_shape_kernels(gpu, shape, dtype, dense):
+    """Register sliding-window kernels (compile-time shapes): bit-exact with dense weights and with
+    exact-zero weights (FP64 then takes the non-zero list, FP32 keeps every weight in the chain)."""
+    v, H, L, R, V, T, B = SHAPES[shape]
+    nx, ny, tiles = 256, 128, 2
+    inp = field(nx, ny, 7, dtype)
+    w = weights_for(v, H, V, 7, dtype, zeros=not dense)
+    if dense:
+        w[w == 0] = 0.5
+    pre = sentinel(nx, ny, dtype)
+    ref = pre.copy()
+    st = oracle.stencil(v, ref, inp, w, num_tiles=tiles, block_x=32, block_y=8, H=H, L=L, R=R, V=V, T=T, B=B)
+    d_in, d_out, d_w = DeviceBuffer.from_array(inp), DeviceBuffer.from_array(pre), DeviceBuffer.from_array(w)
+    before = cs.kernel_launches_tma()
+    s = cs.Stencil(v, nx, ny, d_out.ptr, d_in.ptr, d_w.ptr, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=tiles,
+                   block_x=32, block_y=8, dtype=cs.F64 if dtype == np.float64 else cs.F32)
+    s.compute()
+    cs._check(cs.lib().custen_device_synchronize())
+    got = d_out.download((ny, nx), dtype)
+    s.destroy()
+    assert cs.kernel_launches_tma() > before
+    check(got, ref, st, pre)
