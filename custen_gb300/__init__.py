@@ -67,6 +67,18 @@ def lib() -> ctypes.CDLL:
         L.custen_memset.argtypes = [vp, i, sz]
         L.custen_set_device.argtypes = [i]
         L.custen_probe_fma_rate.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.custen_ch_last_error.restype = ctypes.c_char_p
+        L.custen_ch_batch_create.argtypes = [ctypes.POINTER(vp), i, ctypes.POINTER(i), dp, ctypes.c_double,
+                                             ctypes.c_double, i, vp]
+        L.custen_ch_batch_set_state.argtypes = [vp, i, vp, vp]
+        L.custen_ch_batch_get_state.argtypes = [vp, i, vp, vp]
+        L.custen_ch_batch_step.argtypes = [vp, i, i]
+        L.custen_ch_batch_synchronize.argtypes = [vp]
+        L.custen_ch_batch_mean.argtypes = [vp, i, dp]
+        L.custen_ch_batch_launches.argtypes = [vp]
+        L.custen_ch_batch_launches.restype = ull
+        L.custen_ch_batch_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -203,3 +215,69 @@ def create_reference_style(variant: int, nx: int, ny: int, out, inp, coef, *, nu
         ncoef = H * V
     return Stencil(variant, nx, ny, out, inp, coef, H=Hh, L=L, R=R, V=Vv, T=T, B=B, num_tiles=num_tiles,
                    block_x=block_x, block_y=block_y, dtype=dtype, device=device, ncoef=ncoef, func=func)
+
+
+def _ch_check(status: int) -> None:
+    if status != 0:
+        raise CustenError(lib().custen_ch_last_error().decode(errors="replace"))
+
+
+class CahnHilliardBatch:
+    """Many periodic Cahn-Hilliard ADI simulations of different sizes advanced together on the GPU
+    (the solver of cuPentCahnADI, batched; include/custen_gb300.h)."""
+
+    def __init__(self, sizes, lx=None, gamma: float = 0.01, dt_factor: float = 0.1, rhs_dtype: int = F64,
+                 stream=None):
+        import numpy as np
+        self.sizes = [int(n) for n in sizes]
+        ns = (ctypes.c_int * len(self.sizes))(*self.sizes)
+        lxa = None
+        if lx is not None:
+            lxv = [float(v) for v in (lx if hasattr(lx, "__len__") else [lx] * len(self.sizes))]
+            lxa = (ctypes.c_double * len(lxv))(*lxv)
+        h = ctypes.c_void_p()
+        s = stream if (stream is None or isinstance(stream, int)) else int(stream.cuda_stream)
+        _ch_check(lib().custen_ch_batch_create(ctypes.byref(h), len(self.sizes), ns, lxa, gamma, dt_factor, rhs_dtype,
+                                               s))
+        self.h = h.value
+        self._np = np
+
+    def set_state(self, sim: int, c_cur, c_old=None) -> None:
+        np = self._np
+        n = self.sizes[sim]
+        c_cur = np.ascontiguousarray(c_cur, dtype=np.float64).reshape(n, n)
+        c_old = None if c_old is None else np.ascontiguousarray(c_old, dtype=np.float64).reshape(n, n)
+        _ch_check(lib().custen_ch_batch_set_state(self.h, sim, c_cur.ctypes.data,
+                                                  None if c_old is None else c_old.ctypes.data))
+
+    def state(self, sim: int):
+        np = self._np
+        n = self.sizes[sim]
+        cur, old = np.empty((n, n)), np.empty((n, n))
+        _ch_check(lib().custen_ch_batch_get_state(self.h, sim, cur.ctypes.data, old.ctypes.data))
+        return cur, old
+
+    def step(self, steps: int = 1, graph: bool = True) -> None:
+        _ch_check(lib().custen_ch_batch_step(self.h, steps, int(graph)))
+
+    def synchronize(self) -> None:
+        _ch_check(lib().custen_ch_batch_synchronize(self.h))
+
+    def mean(self, sim: int) -> float:
+        m = ctypes.c_double()
+        _ch_check(lib().custen_ch_batch_mean(self.h, sim, ctypes.byref(m)))
+        return float(m.value)
+
+    def launches(self) -> int:
+        return int(lib().custen_ch_batch_launches(self.h))
+
+    def close(self) -> None:
+        if self.h:
+            lib().custen_ch_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,702 @@
+// Cahn-Hilliard ADI solver on sm_103a: one time step of many periodic grids of different sizes.
+//
+// Scheme of the reference solver (cuPentCahnADI/src/cuPentCahnADI.cu:528-596, and its CPU twin
+// cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c:1010-1047), per grid of n x n points:
+//   cBar = 2 cCurr - cOld
+//   rhs  = Lin5x5(cBar) + Nl3x3(cCurr^3 - cCurr) - (2/3)(cCurr - cOld)
+//   (1 + s Dx4)(1 + s Dy4) delta = rhs   -- two cyclic pentadiagonal sweeps, x then y, each solved as
+//       the (n-2) x (n-2) banded block (pre-factored, cuPentBatch.cu:35-198) plus the 2 x 2 Schur
+//       complement on the last two unknowns (BatchHyper.cu:195-259, 421-514)
+//   cNew = cBar + delta;  cOld <- cCurr;  cCurr <- cNew
+//
+// GB300 shape: FP64 FMAs (about 2 per clock per SM) bound this solver, not HBM, so the kernels
+// minimise FP64 operations (about 40 per point and step, against about 100 in the reference: exact
+// zero stencil weights skipped, cBar and c^3 - c computed once per point, divisions replaced by
+// reciprocals) and keep every SM sub-partition busy:
+//   K1 ch_rhs_kernel     -- right-hand side, 32 x 32 blocks, lane = column, all points in parallel.
+//   K2 ch_xsolve_kernel  -- x sweep, one warp per 32 rows (lane = row) walking 32-column chunks
+//                           transposed through shared memory; leaves the banded solution y and the
+//                           two corner values of every row.
+//   K3 ch_ysolve_kernel  -- y sweep, one warp per 32 columns (lane = column, coalesced), applying the
+//                           x sweep's rank-2 correction as it reads, then cNew = cBar + delta written
+//                           over cOld (the two field buffers swap roles every step).
+// Each kernel is persistent over a work list that covers all grids (largest first, claimed through
+// an atomic counter), so grids of different sizes share one launch. A step is three launches; pairs
+// of steps are captured in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/custen_gb300.h"
+
+namespace custen {
+namespace ch {
+
+constexpr int BLK = 32;   // rows / columns per work item; n must be a multiple of 32
+
+// Per-grid descriptor (device).
+struct GridDev {
+    double* buf[2];       // the two field buffers: cCurr = buf[parity], cOld = buf[parity ^ 1]
+    double* tmp;          // n x n work field (rhs, then the x-sweep solution)
+    double* ends;         // 2 n values: the x sweep's last two unknowns of every row
+    const double* tab;    // solver table for n (layout below)
+    int n;
+    int pad;
+};
+
+// Table layout for one n (m = n - 2), all double:
+//   [0, m) ds  [m, 2m) dl  [2m, 3m) rd = 1/diag  [3m, 4m) du  [4m, 5m) dw   (factored, zero-padded:
+//   ds[0] = ds[1] = dl[0] = 0, du[m-1] = 0, dw[m-2] = dw[m-1] = 0)
+//   [5m, 6m) inv1  [6m, 7m) inv2   border columns of the cyclic correction
+//   [7m, 7m+4) omega  [7m+4, 7m+8) a, b, d, e  [7m+8, 7m+33) linear 5x5 weights  [7m+33, 7m+42) the
+//   non-linear 3x3 weights
+__host__ __device__ inline int tab_size(int n) { return 7 * (n - 2) + 42; }
+
+struct Item {
+    int grid;
+    int block;   // K1: 32 x 32 block index (row-major over the grid); K2: row block; K3: column block
+};
+
+// ------------------------------------------------------------------------------------------------
+// K1: right-hand side
+// ------------------------------------------------------------------------------------------------
+// T = double: FP64 arithmetic; T = float: the FP32 precision variant (inputs and weights rounded to
+// float, result widened back to double for the FP64 solve).
+template <typename T>
+__global__ void __launch_bounds__(BLK) ch_rhs_kernel(const GridDev* __restrict__ grids, const Item* __restrict__ items,
+                                                     int n_items, int parity, unsigned int* counter) {
+    __shared__ T cb[36][37];   // cBar over the block and a 2-point halo
+    __shared__ T gg[34][35];   // c^3 - c over the block and a 1-point halo
+    __shared__ T dco[32][33];  // cCurr - cOld at the block's points
+    __shared__ int s_item;
+    const int lane = threadIdx.x;
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        // selects rather than gd.buf[parity]: a run-time index would put the descriptor in local memory
+        const double* cur = parity ? gd.buf[1] : gd.buf[0];
+        const double* old = parity ? gd.buf[0] : gd.buf[1];
+        const double* tab = gd.tab;
+        const int bpr = n / BLK;
+        const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
+        // weights (identical for every lane: broadcast loads)
+        T wl[13], wn[5];
+        {
+            const double* L = tab + 7 * m + 8;
+            const double* N = tab + 7 * m + 33;
+            // non-zero entries of the biharmonic 5x5 and the 3x3 Laplacian, in weight order
+            wl[0] = (T)L[2]; wl[1] = (T)L[6]; wl[2] = (T)L[7]; wl[3] = (T)L[8]; wl[4] = (T)L[10];
+            wl[5] = (T)L[11]; wl[6] = (T)L[12]; wl[7] = (T)L[13]; wl[8] = (T)L[14]; wl[9] = (T)L[16];
+            wl[10] = (T)L[17]; wl[11] = (T)L[18]; wl[12] = (T)L[22];
+            wn[0] = (T)N[1]; wn[1] = (T)N[3]; wn[2] = (T)N[4]; wn[3] = (T)N[5]; wn[4] = (T)N[7];
+        }
+        // stage the 36 x 36 window (periodic wrap)
+#pragma unroll 4
+        for (int e = lane; e < 36 * 36; e += BLK) {
+            const int r = e / 36, c = e - r * 36;
+            int gy = y0 - 2 + r, gx = x0 - 2 + c;
+            gy = gy < 0 ? gy + n : (gy >= n ? gy - n : gy);
+            gx = gx < 0 ? gx + n : (gx >= n ? gx - n : gx);
+            const double cv = cur[(size_t)gy * n + gx];
+            const double ov = old[(size_t)gy * n + gx];
+            const T c32 = (T)cv, o32 = (T)ov;
+            cb[r][c] = fma((T)2, c32, -o32);
+            if (r >= 1 && r < 35 && c >= 1 && c < 35) gg[r - 1][c - 1] = fma(c32 * c32, c32, -c32);
+            if (r >= 2 && r < 34 && c >= 2 && c < 34) dco[r - 2][c - 2] = c32 - o32;
+        }
+        __syncwarp();
+        // lane = column of the block, loop over its 32 rows
+        const int j = lane;
+        double* out = gd.tmp + (size_t)y0 * n + x0 + j;
+#pragma unroll 4
+        for (int rr = 0; rr < BLK; ++rr) {
+            // biharmonic: rows of the 5x5 window, non-zero weights only (the zero ones are exact no-ops)
+            T lin = (T)0;
+            lin = fma(wl[0], cb[rr][j + 2], lin);
+            lin = fma(wl[1], cb[rr + 1][j + 1], lin);
+            lin = fma(wl[2], cb[rr + 1][j + 2], lin);
+            lin = fma(wl[3], cb[rr + 1][j + 3], lin);
+            lin = fma(wl[4], cb[rr + 2][j], lin);
+            lin = fma(wl[5], cb[rr + 2][j + 1], lin);
+            lin = fma(wl[6], cb[rr + 2][j + 2], lin);
+            lin = fma(wl[7], cb[rr + 2][j + 3], lin);
+            lin = fma(wl[8], cb[rr + 2][j + 4], lin);
+            lin = fma(wl[9], cb[rr + 3][j + 1], lin);
+            lin = fma(wl[10], cb[rr + 3][j + 2], lin);
+            lin = fma(wl[11], cb[rr + 3][j + 3], lin);
+            lin = fma(wl[12], cb[rr + 4][j + 2], lin);
+            T nl = (T)0;
+            nl = fma(wn[0], gg[rr][j + 1], nl);
+            nl = fma(wn[1], gg[rr + 1][j], nl);
+            nl = fma(wn[2], gg[rr + 1][j + 1], nl);
+            nl = fma(wn[3], gg[rr + 1][j + 2], nl);
+            nl = fma(wn[4], gg[rr + 2][j + 1], nl);
+            // findRHS: cHalf += -(2/3)(cCurr - cOld) + cNonLinRHS  (cuPentCahnADI.cu:72-86)
+            const T rhs = lin + fma((T)(-2.0 / 3.0), dco[rr][j], nl);
+            out[(size_t)rr * n] = (double)rhs;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// K2: x sweep (lane = row), 32-column chunks through shared memory
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restrict__ grids,
+                                                        const Item* __restrict__ items, int n_items,
+                                                        unsigned int* counter) {
+    __shared__ double blk[BLK][BLK + 1];
+    __shared__ int s_item;
+    const int lane = threadIdx.x;
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* tab = gd.tab;
+        const double* ds = tab;
+        const double* dl = tab + m;
+        const double* rd = tab + 2 * m;
+        const double* du = tab + 3 * m;
+        const double* dw = tab + 4 * m;
+        double* rows = gd.tmp + (size_t)item.block * BLK * n;   // 32 rows, stride n
+        const int nchunk = n / BLK;
+        // forward elimination of the banded (n-2) x (n-2) block, row = lane
+        double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
+        for (int ch = 0; ch < nchunk; ++ch) {
+            const int cx = ch * BLK;
+#pragma unroll 8
+            for (int rr = 0; rr < BLK; ++rr) blk[rr][lane] = rows[(size_t)rr * n + cx + lane];
+            __syncwarp();
+#pragma unroll 4
+            for (int k = 0; k < BLK; ++k) {
+                const int i = cx + k;
+                const double v = blk[lane][k];
+                if (i < m) {
+                    double t = fma(-ds[i], b2, v);
+                    t = fma(-dl[i], b1, t);
+                    t *= rd[i];
+                    b2 = b1;
+                    b1 = t;
+                    blk[lane][k] = t;
+                } else if (i == m) {
+                    r2 = v;
+                } else {
+                    r1 = v;
+                }
+            }
+            __syncwarp();
+#pragma unroll 8
+            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + cx + lane] = blk[rr][lane];
+            __syncwarp();
+        }
+        // backward substitution, chunks in reverse
+        double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
+        for (int ch = nchunk - 1; ch >= 0; --ch) {
+            const int cx = ch * BLK;
+#pragma unroll 8
+            for (int rr = 0; rr < BLK; ++rr) blk[rr][lane] = rows[(size_t)rr * n + cx + lane];
+            __syncwarp();
+#pragma unroll 4
+            for (int k = BLK - 1; k >= 0; --k) {
+                const int i = cx + k;
+                if (i < m) {
+                    double y = fma(-du[i], f1, blk[lane][k]);
+                    y = fma(-dw[i], f2, y);
+                    f2 = f1;
+                    f1 = y;
+                    blk[lane][k] = y;
+                    if (i == 0) y0v = y;
+                    if (i == 1) y1v = y;
+                    if (i == m - 2) ym2 = y;
+                    if (i == m - 1) ym1 = y;
+                }
+            }
+            __syncwarp();
+#pragma unroll 8
+            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + cx + lane] = blk[rr][lane];
+            __syncwarp();
+        }
+        // the last two unknowns through the 2 x 2 Schur complement (BatchHyper.cu:195-227)
+        const double* om = tab + 7 * m;
+        const double a = om[4], b = om[5], d = om[6], e = om[7];
+        const double nx2 = r2 - (e * y0v + a * ym2 + b * ym1);
+        const double nx1 = r1 - (d * y0v + e * y1v + a * ym1);
+        double* row = rows + (size_t)lane * n;
+        const double x2 = om[0] * nx2 + om[1] * nx1;
+        const double x1 = om[2] * nx2 + om[3] * nx1;
+        row[n - 2] = x2;
+        row[n - 1] = x1;
+        // kept apart as well: the y sweep overwrites columns n-2 and n-1 of tmp while other warps still
+        // need them for the rank-2 correction
+        const int gy = item.block * BLK + lane;
+        gd.ends[2 * gy] = x2;
+        gd.ends[2 * gy + 1] = x1;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// K3: y sweep (lane = column) + the update
+// ------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restrict__ grids,
+                                                        const Item* __restrict__ items, int n_items, int parity,
+                                                        unsigned int* counter) {
+    __shared__ int s_item;
+    const int lane = threadIdx.x;
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* tab = gd.tab;
+        const double* ds = tab;
+        const double* dl = tab + m;
+        const double* rd = tab + 2 * m;
+        const double* du = tab + 3 * m;
+        const double* dw = tab + 4 * m;
+        const double* inv1 = tab + 5 * m;
+        const double* inv2 = tab + 6 * m;
+        const int x = item.block * BLK + lane;
+        double* t = gd.tmp;
+        // x sweep's rank-2 correction for this column (BatchHyper.cu:233-259): applied on read
+        const double cx1 = (x < m) ? inv1[x] : 0.0;
+        const double cx2 = (x < m) ? inv2[x] : 0.0;
+        const double* ends = gd.ends;
+        const bool corr = x < m;
+#define CH_XVAL(y) (corr ? fma(-cx1, ends[2 * (y)], fma(-cx2, ends[2 * (y) + 1], t[(size_t)(y) * n + x])) \
+                         : t[(size_t)(y) * n + x])
+        // forward elimination along y
+        double b1 = 0.0, b2 = 0.0;
+#pragma unroll 4
+        for (int y = 0; y < m; ++y) {
+            double v = fma(-ds[y], b2, CH_XVAL(y));
+            v = fma(-dl[y], b1, v);
+            v *= rd[y];
+            b2 = b1;
+            b1 = v;
+            t[(size_t)y * n + x] = v;
+        }
+        const double r2 = CH_XVAL(m), r1 = CH_XVAL(m + 1);
+#undef CH_XVAL
+        // backward substitution
+        double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
+#pragma unroll 4
+        for (int y = m - 1; y >= 0; --y) {
+            double v = fma(-du[y], f1, t[(size_t)y * n + x]);
+            v = fma(-dw[y], f2, v);
+            f2 = f1;
+            f1 = v;
+            t[(size_t)y * n + x] = v;
+            if (y == m - 1) ym1 = v;
+            if (y == m - 2) ym2 = v;
+            if (y == 1) y1v = v;
+            if (y == 0) y0v = v;
+        }
+        const double* om = tab + 7 * m;
+        const double a = om[4], b = om[5], d = om[6], e = om[7];
+        const double nx2 = r2 - (e * y0v + a * ym2 + b * ym1);
+        const double nx1 = r1 - (d * y0v + e * y1v + a * ym1);
+        const double x2 = om[0] * nx2 + om[1] * nx1;
+        const double x1 = om[2] * nx2 + om[3] * nx1;
+        // cNew = cBar + delta over cOld (cuPentCahnADI.cu:58-69, 89-100)
+        const double* cur = parity ? gd.buf[1] : gd.buf[0];
+        double* old = parity ? gd.buf[0] : gd.buf[1];
+#pragma unroll 4
+        for (int y = 0; y < n; ++y) {
+            const size_t k = (size_t)y * n + x;
+            double dlt;
+            if (y < m) dlt = fma(-inv1[y], x2, fma(-inv2[y], x1, t[k]));
+            else dlt = (y == m) ? x2 : x1;
+            const double cbar = fma(2.0, cur[k], -old[k]);
+            old[k] = cbar + dlt;
+        }
+    }
+}
+
+// Compensated (Neumaier) sum of one grid, one CTA of 256 threads; combined with a two-sum tree.
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& err) {
+    s = a + b;
+    const double bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+}
+
+__global__ void __launch_bounds__(256) ch_mass_kernel(const double* __restrict__ f, long long count, double* out) {
+    __shared__ double ss[256], sc[256];
+    double s = 0.0, c = 0.0;
+    for (long long k = threadIdx.x; k < count; k += blockDim.x) {
+        double t, e;
+        two_sum(s, f[k], t, e);
+        s = t;
+        c += e;
+    }
+    ss[threadIdx.x] = s;
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            double t, e;
+            two_sum(ss[threadIdx.x], ss[threadIdx.x + w], t, e);
+            ss[threadIdx.x] = t;
+            sc[threadIdx.x] += sc[threadIdx.x + w] + e;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = ss[0] + sc[0];
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------------
+
+// Solver table for an n x n grid of side lx with D = 1, gamma, dt = dt_factor * dx (the reference
+// defaults are gamma = 0.01, dt = 0.1 dx: cuPentCahnADI.cu:204-221).
+static std::vector<double> build_table(int n, double lx, double gamma, double dt_factor) {
+    const int m = n - 2;
+    const double D = 1.0, dx = lx / n, dt = dt_factor * dx;
+    const double sl = 2.0 * dt * D * gamma / (3.0 * (dx * dx * dx * dx));
+    const double a = sl, b = -4 * sl, c = 1 + 6 * sl, d = -4 * sl, e = sl;
+    std::vector<double> ds(m, 0.0), dl(m, 0.0), dg(m, c), du(m, 0.0), dw(m, 0.0);
+    for (int i = 0; i < m; ++i) {
+        if (i > 1) ds[i] = a;
+        if (i > 0) dl[i] = b;
+        if (i < m - 1) du[i] = d;
+        if (i < m - 2) dw[i] = e;
+    }
+    // in-place factorisation of the banded block (cuPentBatch.cu:35-113)
+    auto factor = [m](std::vector<double>& s_, std::vector<double>& l_, std::vector<double>& g_,
+                      std::vector<double>& u_, std::vector<double>& w_) {
+        u_[0] = u_[0] / g_[0];
+        w_[0] = w_[0] / g_[0];
+        g_[1] = g_[1] - l_[1] * u_[0];
+        u_[1] = (u_[1] - l_[1] * w_[0]) / g_[1];
+        w_[1] = w_[1] / g_[1];
+        for (int i = 2; i < m; ++i) {
+            l_[i] = l_[i] - s_[i] * u_[i - 2];
+            g_[i] = g_[i] - s_[i] * w_[i - 2] - l_[i] * u_[i - 1];
+            if (i < m - 2) w_[i] = w_[i] / g_[i];
+            if (i < m - 1) u_[i] = (u_[i] - l_[i] * w_[i - 1]) / g_[i];
+        }
+    };
+    factor(ds, dl, dg, du, dw);
+    auto solve = [&](std::vector<double>& x) {
+        x[0] = x[0] / dg[0];
+        x[1] = (x[1] - dl[1] * x[0]) / dg[1];
+        for (int i = 2; i < m; ++i) x[i] = (x[i] - ds[i] * x[i - 2] - dl[i] * x[i - 1]) / dg[i];
+        x[m - 2] = x[m - 2] - du[m - 2] * x[m - 1];
+        for (int i = m - 3; i >= 0; --i) x[i] = x[i] - du[i] * x[i + 1] - dw[i] * x[i + 2];
+    };
+    // border columns and omega (BatchHyper.cu:421-514)
+    std::vector<double> inv1(m, 0.0), inv2(m, 0.0);
+    inv1[0] = a; inv1[m - 2] = e; inv1[m - 1] = d;
+    inv2[0] = b; inv2[1] = a; inv2[m - 1] = e;
+    solve(inv1);
+    solve(inv2);
+    const double z11 = e * inv1[0] + a * inv1[m - 2] + b * inv1[m - 1];
+    const double z12 = e * inv2[0] + a * inv2[m - 2] + b * inv2[m - 1];
+    const double z21 = d * inv1[0] + e * inv1[1] + a * inv1[m - 1];
+    const double z22 = d * inv2[0] + e * inv2[1] + a * inv2[m - 1];
+    const double y11 = c - z11, y12 = d - z12, y21 = b - z21, y22 = c - z22;
+    const double det = 1.0 / (y11 * y22 - y21 * y12);
+    std::vector<double> t(tab_size(n), 0.0);
+    for (int i = 0; i < m; ++i) {
+        t[i] = (i > 1) ? ds[i] : 0.0;
+        t[m + i] = (i > 0) ? dl[i] : 0.0;
+        t[2 * m + i] = 1.0 / dg[i];
+        t[3 * m + i] = (i < m - 1) ? du[i] : 0.0;
+        t[4 * m + i] = (i < m - 2) ? dw[i] : 0.0;
+        t[5 * m + i] = inv1[i];
+        t[6 * m + i] = inv2[i];
+    }
+    double* om = &t[7 * m];
+    om[0] = y22 * det;
+    om[1] = -y12 * det;
+    om[2] = -y21 * det;
+    om[3] = y11 * det;
+    om[4] = a; om[5] = b; om[6] = d; om[7] = e;
+    static const double wl[25] = {0, 0, -1, 0, 0, 0, -2, 8, -2, 0, -1, 8, -20, 8, -1, 0, -2, 8, -2, 0, 0, 0, -1, 0, 0};
+    static const double wn[9] = {0, 1, 0, 1, -4, 1, 0, 1, 0};
+    const double snl = (dt / 3.0) * D * (2.0 / (dx * dx));
+    for (int k = 0; k < 25; ++k) t[7 * m + 8 + k] = wl[k] * sl;
+    for (int k = 0; k < 9; ++k) t[7 * m + 33 + k] = wn[k] * snl;
+    return t;
+}
+
+struct Batch {
+    int device = 0;
+    int rhs_fp32 = 0;
+    int parity = 0;   // cCurr = buf[parity]
+    long long steps_done = 0;
+    std::vector<int> n;
+    std::vector<double> lx;
+    std::vector<GridDev> grids_h;
+    std::vector<double*> allocs;
+    std::vector<std::pair<std::string, double*>> tables;   // key "n/lx/gamma/dtf" -> device table
+    GridDev* grids_d = nullptr;
+    Item* items_rhs = nullptr;
+    Item* items_rows = nullptr;   // K2 and K3 share the per-grid block lists (row / column blocks)
+    int n_items_rhs = 0, n_items_rows = 0;
+    unsigned int* counters = nullptr;   // 3 counters per step of a captured pair
+    double* mass_d = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};   // pair of steps starting at parity 0 / 1
+    int grid_k1 = 0, grid_k23 = 0;
+    unsigned long long launches = 0;
+};
+
+static thread_local std::string g_ch_err;
+static int ch_fail(cudaError_t e, const char* what) {
+    g_ch_err = std::string("Error while '") + what + "': " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return 1;
+}
+static int ch_fail_arg(const std::string& msg) {
+    g_ch_err = msg;
+    return 2;
+}
+#define CH_TRY(x, what)                             \
+    do {                                            \
+        cudaError_t _e = (x);                       \
+        if (_e != cudaSuccess) return ch_fail(_e, what); \
+    } while (0)
+
+static int enqueue_step(Batch* b, int parity, int slot) {
+    unsigned int* ctr = b->counters + 3 * slot;
+    CH_TRY(cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned int), b->stream), "Resetting work counters");
+    if (b->rhs_fp32)
+        ch_rhs_kernel<float><<<b->grid_k1, BLK, 0, b->stream>>>(b->grids_d, b->items_rhs, b->n_items_rhs, parity,
+                                                                ctr);
+    else
+        ch_rhs_kernel<double><<<b->grid_k1, BLK, 0, b->stream>>>(b->grids_d, b->items_rhs, b->n_items_rhs, parity,
+                                                                 ctr);
+    CH_TRY(cudaGetLastError(), "Launching right-hand side");
+    ch_xsolve_kernel<<<b->grid_k23, BLK, 0, b->stream>>>(b->grids_d, b->items_rows, b->n_items_rows, ctr + 1);
+    CH_TRY(cudaGetLastError(), "Launching x sweep");
+    ch_ysolve_kernel<<<b->grid_k23, BLK, 0, b->stream>>>(b->grids_d, b->items_rows, b->n_items_rows, parity, ctr + 2);
+    CH_TRY(cudaGetLastError(), "Launching y sweep");
+    return 0;
+}
+
+static int capture_pairs(Batch* b) {
+    for (int p = 0; p < 2; ++p) {
+        if (b->graph_exec[p]) continue;
+        cudaGraph_t g;
+        CH_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "Beginning graph capture");
+        int st = enqueue_step(b, p, 0);
+        if (st == 0) st = enqueue_step(b, p ^ 1, 1);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (st != 0) return st;
+        CH_TRY(e, "Ending graph capture");
+        e = cudaGraphInstantiate(&b->graph_exec[p], g, 0);
+        cudaGraphDestroy(g);
+        CH_TRY(e, "Instantiating graph");
+    }
+    return 0;
+}
+
+}  // namespace ch
+}  // namespace custen
+
+using namespace custen::ch;
+
+extern "C" {
+
+const char* custen_ch_last_error(void) { return g_ch_err.c_str(); }
+
+int custen_ch_batch_create(void** out, int nsims, const int* n, const double* lx, double gamma, double dt_factor,
+                           int rhs_dtype, void* stream) {
+    if (!out || nsims < 1 || !n) return ch_fail_arg("invalid arguments");
+    for (int s = 0; s < nsims; ++s)
+        if (n[s] < 64 || n[s] % BLK != 0) return ch_fail_arg("grid sizes must be multiples of 32, at least 64");
+    Batch* b = new Batch();
+    cudaGetDevice(&b->device);
+    b->rhs_fp32 = rhs_dtype == CUSTEN_F32;
+    if (stream) {
+        b->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete b; return ch_fail(e, "Creating stream"); }
+        b->own_stream = true;
+    }
+    auto cleanup_fail = [&](int st) {
+        for (double* p : b->allocs) cudaFree(p);
+        for (auto& t : b->tables) cudaFree(t.second);
+        if (b->own_stream) cudaStreamDestroy(b->stream);
+        delete b;
+        return st;
+    };
+    b->n.assign(n, n + nsims);
+    b->lx.resize(nsims);
+    for (int s = 0; s < nsims; ++s) b->lx[s] = lx ? lx[s] : 2.0 * M_PI;
+    b->grids_h.resize(nsims);
+    for (int s = 0; s < nsims; ++s) {
+        const int ns = n[s];
+        char key[128];
+        snprintf(key, sizeof(key), "%d/%.17g/%.17g/%.17g", ns, b->lx[s], gamma, dt_factor);
+        double* tab = nullptr;
+        for (auto& t : b->tables)
+            if (t.first == key) tab = t.second;
+        if (!tab) {
+            std::vector<double> h = build_table(ns, b->lx[s], gamma, dt_factor);
+            cudaError_t e = cudaMalloc(&tab, h.size() * sizeof(double));
+            if (e != cudaSuccess) return cleanup_fail(ch_fail(e, "Allocating solver table"));
+            e = cudaMemcpy(tab, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cleanup_fail(ch_fail(e, "Uploading solver table"));
+            b->tables.push_back({key, tab});
+        }
+        GridDev g{};
+        const size_t bytes = (size_t)ns * ns * sizeof(double);
+        for (int k = 0; k < 4; ++k) {
+            double* p = nullptr;
+            cudaError_t e = cudaMalloc(&p, k < 3 ? bytes : 2 * ns * sizeof(double));
+            if (e != cudaSuccess) return cleanup_fail(ch_fail(e, "Allocating grid fields"));
+            b->allocs.push_back(p);
+            if (k < 2) g.buf[k] = p; else if (k == 2) g.tmp = p; else g.ends = p;
+        }
+        g.tab = tab;
+        g.n = ns;
+        b->grids_h[s] = g;
+    }
+    // work lists, largest grids first
+    std::vector<int> order(nsims);
+    for (int s = 0; s < nsims; ++s) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+    std::vector<Item> rhs, rows;
+    for (int s : order) {
+        const int bpr = n[s] / BLK;
+        for (int k = 0; k < bpr * bpr; ++k) rhs.push_back({s, k});
+        for (int k = 0; k < bpr; ++k) rows.push_back({s, k});
+    }
+    b->n_items_rhs = (int)rhs.size();
+    b->n_items_rows = (int)rows.size();
+    cudaError_t e = cudaMalloc(&b->grids_d, nsims * sizeof(GridDev));
+    if (e == cudaSuccess) e = cudaMemcpy(b->grids_d, b->grids_h.data(), nsims * sizeof(GridDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->items_rhs, rhs.size() * sizeof(Item));
+    if (e == cudaSuccess) e = cudaMemcpy(b->items_rhs, rhs.data(), rhs.size() * sizeof(Item), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->items_rows, rows.size() * sizeof(Item));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->items_rows, rows.data(), rows.size() * sizeof(Item), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->counters, 6 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->mass_d, sizeof(double));
+    if (e != cudaSuccess) return cleanup_fail(ch_fail(e, "Allocating work lists"));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    // one warp per CTA, enough CTAs to give every SM sub-partition several warps
+    b->grid_k1 = std::min(b->n_items_rhs, sms * 16);
+    b->grid_k23 = std::min(b->n_items_rows, sms * 16);
+    *out = b;
+    return 0;
+}
+
+int custen_ch_batch_set_state(void* h, int sim, const double* c_cur, const double* c_old) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || sim < 0 || sim >= (int)b->n.size() || !c_cur) return ch_fail_arg("invalid arguments");
+    const size_t bytes = (size_t)b->n[sim] * b->n[sim] * sizeof(double);
+    GridDev& g = b->grids_h[sim];
+    CH_TRY(cudaMemcpyAsync(g.buf[b->parity], c_cur, bytes, cudaMemcpyDefault, b->stream), "Uploading cCurr");
+    CH_TRY(cudaMemcpyAsync(g.buf[b->parity ^ 1], c_old ? c_old : c_cur, bytes, cudaMemcpyDefault, b->stream),
+           "Uploading cOld");
+    CH_TRY(cudaStreamSynchronize(b->stream), "Synchronising upload");
+    return 0;
+}
+
+int custen_ch_batch_get_state(void* h, int sim, double* c_cur, double* c_old) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || sim < 0 || sim >= (int)b->n.size()) return ch_fail_arg("invalid arguments");
+    const size_t bytes = (size_t)b->n[sim] * b->n[sim] * sizeof(double);
+    GridDev& g = b->grids_h[sim];
+    if (c_cur) CH_TRY(cudaMemcpyAsync(c_cur, g.buf[b->parity], bytes, cudaMemcpyDefault, b->stream), "Reading cCurr");
+    if (c_old)
+        CH_TRY(cudaMemcpyAsync(c_old, g.buf[b->parity ^ 1], bytes, cudaMemcpyDefault, b->stream), "Reading cOld");
+    CH_TRY(cudaStreamSynchronize(b->stream), "Synchronising read");
+    return 0;
+}
+
+// Advance every grid by `steps` steps; asynchronous on the batch's stream (graph replays for pairs of
+// steps, plain launches for an odd remainder) unless use_graph == 0.
+int custen_ch_batch_step(void* h, int steps, int use_graph) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || steps < 0) return ch_fail_arg("invalid arguments");
+    cudaSetDevice(b->device);
+    int left = steps;
+    if (use_graph && left >= 2) {
+        int st = capture_pairs(b);
+        if (st) return st;
+        while (left >= 2) {
+            CH_TRY(cudaGraphLaunch(b->graph_exec[b->parity], b->stream), "Launching step graph");
+            b->launches += 6;
+            left -= 2;
+            b->steps_done += 2;
+        }
+    }
+    while (left > 0) {
+        int st = enqueue_step(b, b->parity, 0);
+        if (st) return st;
+        b->launches += 3;
+        b->parity ^= 1;
+        --left;
+        ++b->steps_done;
+    }
+    return 0;
+}
+
+int custen_ch_batch_synchronize(void* h) {
+    Batch* b = static_cast<Batch*>(h);
+    CH_TRY(cudaStreamSynchronize(b->stream), "Synchronising batch");
+    return 0;
+}
+
+// Mean of a grid's cCurr with a compensated FP64 sum (device side).
+int custen_ch_batch_mean(void* h, int sim, double* mean) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || sim < 0 || sim >= (int)b->n.size() || !mean) return ch_fail_arg("invalid arguments");
+    const long long count = (long long)b->n[sim] * b->n[sim];
+    ch_mass_kernel<<<1, 256, 0, b->stream>>>(b->grids_h[sim].buf[b->parity], count, b->mass_d);
+    CH_TRY(cudaGetLastError(), "Launching mass sum");
+    double s = 0.0;
+    CH_TRY(cudaMemcpyAsync(&s, b->mass_d, sizeof(double), cudaMemcpyDeviceToHost, b->stream), "Reading mass");
+    CH_TRY(cudaStreamSynchronize(b->stream), "Synchronising mass");
+    *mean = s / (double)count;
+    return 0;
+}
+
+unsigned long long custen_ch_batch_launches(void* h) { return static_cast<Batch*>(h)->launches; }
+
+int custen_ch_batch_destroy(void* h) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b) return 0;
+    cudaStreamSynchronize(b->stream);
+    for (int p = 0; p < 2; ++p)
+        if (b->graph_exec[p]) cudaGraphExecDestroy(b->graph_exec[p]);
+    for (double* p : b->allocs) cudaFree(p);
+    for (auto& t : b->tables) cudaFree(t.second);
+    cudaFree(b->grids_d);
+    cudaFree(b->items_rhs);
+    cudaFree(b->items_rows);
+    cudaFree(b->counters);
+    cudaFree(b->mass_d);
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return 0;
+}
+
+}  // extern "C"

@@ -124,6 +124,23 @@ int custen_probe_fma_rate(int dtype, double* fma_per_s);
  * No counterpart in the reference (its kernels have no waits). */
 int custen_device_error(unsigned int* flags, int clear);
 
+/* ---- Cahn-Hilliard ADI solver: batches of periodic grids of different sizes ----
+ * The method of cuPentCahnADI (cuPentCahnADI/src/cuPentCahnADI.cu:197-627 with BatchHyper.cu and
+ * cuPentBatch.cu): D = 1, gamma, dt = dt_factor * dx, domain [0, lx)^2, BDF2 / ADI with cyclic
+ * pentadiagonal sweeps. Grid sizes n: multiples of 32, at least 64. lx may be NULL (2 pi each).
+ * rhs_dtype CUSTEN_F32 computes the explicit stencil terms in FP32 (precision variant); the solves,
+ * updates and mass sums stay FP64. State arrays are n*n doubles, host or device pointers. */
+const char* custen_ch_last_error(void);
+int custen_ch_batch_create(void** batch, int nsims, const int* n, const double* lx, double gamma, double dt_factor,
+                           int rhs_dtype, void* stream);
+int custen_ch_batch_set_state(void* batch, int sim, const double* c_cur, const double* c_old);
+int custen_ch_batch_get_state(void* batch, int sim, double* c_cur, double* c_old);
+int custen_ch_batch_step(void* batch, int steps, int use_graph);   /* asynchronous */
+int custen_ch_batch_synchronize(void* batch);
+int custen_ch_batch_mean(void* batch, int sim, double* mean);     /* compensated FP64 sum */
+unsigned long long custen_ch_batch_launches(void* batch);
+int custen_ch_batch_destroy(void* batch);
+
 /* ---- memory helpers for hosts without a CUDA runtime binding ---- */
 int custen_malloc_managed(void** ptr, size_t bytes);
 int custen_malloc_device(void** ptr, size_t bytes);

@@ -74,6 +74,14 @@ def lib() -> ctypes.CDLL:
             f.restype = i
         L.oracle_host_loop_xyp_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i]
         L.oracle_host_loop_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i, i]
+        L.ch_oracle_create.argtypes = [i, ctypes.c_double, vp]
+        L.ch_oracle_create.restype = vp
+        L.ch_oracle_step.argtypes = [vp, i]
+        L.ch_oracle_get.argtypes = [vp, vp, vp]
+        L.ch_oracle_tables.argtypes = [vp, vp]
+        L.ch_oracle_destroy.argtypes = [vp]
+        L.ch_oracle_mean.argtypes = [vp, ctypes.c_longlong]
+        L.ch_oracle_mean.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -115,6 +123,61 @@ def host_loop(inp: np.ndarray, out: np.ndarray, w: np.ndarray, H: int, L: int, V
     ny, nx = inp.shape
     lib().oracle_host_loop_f64(nx, ny, _p(inp), _p(out), _p(np.ascontiguousarray(w, dtype=np.float64)), H, L, V, T,
                                int(cube), y0, y1)
+
+
+class CHOracle:
+    """The C restatement of the serial Cahn-Hilliard ADI solver (ch_oracle.c)."""
+
+    def __init__(self, c0: np.ndarray, lx: float = 2 * np.pi):
+        L = lib()
+        n = c0.shape[0]
+        assert c0.shape == (n, n)
+        self.n = n
+        self._c0 = np.ascontiguousarray(c0, dtype=np.float64)
+        self._h = L.ch_oracle_create(n, lx, _p(self._c0))
+
+    def step(self, steps: int = 1) -> None:
+        lib().ch_oracle_step(self._h, steps)
+
+    def fields(self):
+        cur = np.empty((self.n, self.n))
+        old = np.empty((self.n, self.n))
+        lib().ch_oracle_get(self._h, _p(cur), _p(old))
+        return cur, old
+
+    def tables(self) -> np.ndarray:
+        m = self.n - 2
+        out = np.empty(7 * m + 4)
+        lib().ch_oracle_tables(self._h, _p(out))
+        return out
+
+    def __del__(self):
+        try:
+            lib().ch_oracle_destroy(self._h)
+        except Exception:
+            pass
+
+
+def compensated_mean(c: np.ndarray) -> float:
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    return float(lib().ch_oracle_mean(_p(c), c.size))
+
+
+SERIAL_REF = HERE / "_ref" / "libserialch.so"
+
+
+def reference_serial_ch(c0: np.ndarray, steps: int, lx: float = 2 * np.pi):
+    """The reference's own serialCahnADI.c functions (built from its source); None if not built."""
+    if not SERIAL_REF.exists():
+        return None
+    R = ctypes.CDLL(str(SERIAL_REF))
+    R.ref_ch_run.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.c_void_p]
+    n = c0.shape[0]
+    c0 = np.ascontiguousarray(c0, dtype=np.float64)
+    cur, old = np.empty((n, n)), np.empty((n, n))
+    R.ref_ch_run(n, lx, steps, _p(c0), _p(cur), _p(old))
+    return cur, old
 
 
 def reference_kernels():

@@ -1,0 +1,111 @@
+"""Cahn-Hilliard ADI solver (GPU) against the oracle restatement of the reference serial solver.
+
+Tolerances (the reference's own CPU and GPU programs differ in rounding, fused multiply-adds on the
+GPU): relative L2 <= 1e-10 and |mean(c_end) - mean(c0)| <= 1e-12 with a compensated sum.
+"""
+import numpy as np
+import pytest
+
+import custen_gb300 as cs
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+REL_L2 = 1e-10
+MASS = 1e-12
+
+
+def c0_for(n, seed):
+    return np.random.default_rng(seed).uniform(-0.1, 0.1, (n, n))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("n,steps", [(64, 50), (128, 40), (96, 30)])
+def test_single_grid_matches_oracle(gpu, n, steps):
+    c0 = c0_for(n, n)
+    b = cs.CahnHilliardBatch([n])
+    b.set_state(0, c0)
+    b.step(steps)
+    cur, old = b.state(0)
+    ref = oracle.CHOracle(c0)
+    ref.step(steps)
+    rcur, rold = ref.fields()
+    assert rel_l2(cur, rcur) <= REL_L2
+    assert rel_l2(old, rold) <= REL_L2
+    assert abs(b.mean(0) - oracle.compensated_mean(c0)) <= MASS
+    b.close()
+
+
+def test_config1_256_1000_steps(gpu):
+    """The plain method on one 256^2 grid, [0, 2 pi)^2, 1000 steps, c0 ~ U(-0.1, 0.1) seed 0."""
+    n, steps = 256, 1000
+    c0 = c0_for(n, 0)
+    b = cs.CahnHilliardBatch([n])
+    b.set_state(0, c0)
+    b.step(steps)
+    cur, _ = b.state(0)
+    ref = oracle.CHOracle(c0)
+    ref.step(steps)
+    rcur, _ = ref.fields()
+    err = rel_l2(cur, rcur)
+    print(f"256^2 x 1000 steps: rel L2 {err:.3e}, mass drift {abs(b.mean(0) - oracle.compensated_mean(c0)):.3e}")
+    assert err <= REL_L2
+    assert abs(b.mean(0) - oracle.compensated_mean(c0)) <= MASS
+    b.close()
+
+
+def test_batch_equals_alone_and_oracle(gpu):
+    """Uneven grids advanced together give, for each grid, exactly what that grid gives alone."""
+    sizes = [128, 64, 256, 64, 96]
+    steps = 25
+    c0s = [c0_for(n, 10 + k) for k, n in enumerate(sizes)]
+    b = cs.CahnHilliardBatch(sizes)
+    for k, c in enumerate(c0s):
+        b.set_state(k, c)
+    b.step(steps)
+    for k, n in enumerate(sizes):
+        mix, _ = b.state(k)
+        alone = cs.CahnHilliardBatch([n])
+        alone.set_state(0, c0s[k])
+        alone.step(steps)
+        a, _ = alone.state(0)
+        alone.close()
+        assert np.array_equal(mix, a), f"grid {k} differs alone vs in the batch"
+        ref = oracle.CHOracle(c0s[k])
+        ref.step(steps)
+        assert rel_l2(mix, ref.fields()[0]) <= REL_L2
+    b.close()
+
+
+def test_graph_and_plain_launches_agree(gpu):
+    c0 = c0_for(128, 3)
+    outs = []
+    for graph in (True, False):
+        b = cs.CahnHilliardBatch([128, 64])
+        b.set_state(0, c0)
+        b.set_state(1, c0_for(64, 4))
+        b.step(7, graph=graph)
+        outs.append(b.state(0)[0])
+        b.close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_fp32_stencil_variant_error_reported(gpu):
+    """FP32 explicit terms, FP64 solve: the error against the FP64 oracle is bounded and mass holds."""
+    n, steps = 128, 50
+    c0 = c0_for(n, 5)
+    b = cs.CahnHilliardBatch([n], rhs_dtype=cs.F32)
+    b.set_state(0, c0)
+    b.step(steps)
+    cur, _ = b.state(0)
+    ref = oracle.CHOracle(c0)
+    ref.step(steps)
+    err = rel_l2(cur, ref.fields()[0])
+    drift = abs(b.mean(0) - oracle.compensated_mean(c0))
+    print(f"FP32-stencil variant 128^2 x 50: rel L2 {err:.3e}, mass drift {drift:.3e}")
+    assert err < 1e-3
+    assert drift < 1e-6
+    b.close()
