@@ -127,6 +127,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def reduce_max(value: float, dist=None, device=None) -> float:
+    """Max over ranks (the slowest replica sets the job's time)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(points_per_rank: float, world: int, ms_per_step: float) -> float:
+    """Whole-job points per second (weak scaling: every rank processes points_per_rank per step)."""
+    return world * points_per_rank / (ms_per_step * 1e-3)
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -277,13 +292,10 @@ def run_gpu(args, world, rank, local):
     sampler.start()
     total_ms, per_op, launches = timed_sweep(hs64, args.steps, args.warmup)
     clocks = sampler.stop()
-    if pg:
-        t = torch.tensor([total_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(total_ms, pg, dev)
     ms_per_step = total_ms / args.steps
     pts_step = len(ops) * n * n
-    value = world * pts_step / (ms_per_step * 1e-3) / 1e9
+    value = job_throughput(pts_step, world, ms_per_step) / 1e9
 
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs") or 6800.0
