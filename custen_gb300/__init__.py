@@ -79,6 +79,7 @@ def lib() -> ctypes.CDLL:
         L.custen_ch_batch_launches.argtypes = [vp]
         L.custen_ch_batch_launches.restype = ull
         L.custen_ch_batch_destroy.argtypes = [vp]
+        L.custen_ch_step_noalloc.argtypes = [vp, vp, vp, i, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
         _lib = L
     return _lib
 

@@ -368,36 +368,35 @@ __global__ void __launch_bounds__(256) ch_mass_kernel(const double* __restrict__
 // ------------------------------------------------------------------------------------------------
 
 // Solver table for an n x n grid of side lx with D = 1, gamma, dt = dt_factor * dx (the reference
-// defaults are gamma = 0.01, dt = 0.1 dx: cuPentCahnADI.cu:204-221).
-static std::vector<double> build_table(int n, double lx, double gamma, double dt_factor) {
+// defaults are gamma = 0.01, dt = 0.1 dx: cuPentCahnADI.cu:204-221), written into t (tab_size(n)
+// doubles) with `work` (7 * (n - 2) doubles) as scratch.
+static void fill_table(double* t, double* work, int n, double lx, double gamma, double dt_factor) {
     const int m = n - 2;
     const double D = 1.0, dx = lx / n, dt = dt_factor * dx;
     const double sl = 2.0 * dt * D * gamma / (3.0 * (dx * dx * dx * dx));
     const double a = sl, b = -4 * sl, c = 1 + 6 * sl, d = -4 * sl, e = sl;
-    std::vector<double> ds(m, 0.0), dl(m, 0.0), dg(m, c), du(m, 0.0), dw(m, 0.0);
+    double *ds = work, *dl = work + m, *dg = work + 2 * m, *du = work + 3 * m, *dw = work + 4 * m;
+    double *inv1 = work + 5 * m, *inv2 = work + 6 * m;
     for (int i = 0; i < m; ++i) {
-        if (i > 1) ds[i] = a;
-        if (i > 0) dl[i] = b;
-        if (i < m - 1) du[i] = d;
-        if (i < m - 2) dw[i] = e;
+        ds[i] = (i > 1) ? a : 0.0;
+        dl[i] = (i > 0) ? b : 0.0;
+        dg[i] = c;
+        du[i] = (i < m - 1) ? d : 0.0;
+        dw[i] = (i < m - 2) ? e : 0.0;
     }
     // in-place factorisation of the banded block (cuPentBatch.cu:35-113)
-    auto factor = [m](std::vector<double>& s_, std::vector<double>& l_, std::vector<double>& g_,
-                      std::vector<double>& u_, std::vector<double>& w_) {
-        u_[0] = u_[0] / g_[0];
-        w_[0] = w_[0] / g_[0];
-        g_[1] = g_[1] - l_[1] * u_[0];
-        u_[1] = (u_[1] - l_[1] * w_[0]) / g_[1];
-        w_[1] = w_[1] / g_[1];
-        for (int i = 2; i < m; ++i) {
-            l_[i] = l_[i] - s_[i] * u_[i - 2];
-            g_[i] = g_[i] - s_[i] * w_[i - 2] - l_[i] * u_[i - 1];
-            if (i < m - 2) w_[i] = w_[i] / g_[i];
-            if (i < m - 1) u_[i] = (u_[i] - l_[i] * w_[i - 1]) / g_[i];
-        }
-    };
-    factor(ds, dl, dg, du, dw);
-    auto solve = [&](std::vector<double>& x) {
+    du[0] = du[0] / dg[0];
+    dw[0] = dw[0] / dg[0];
+    dg[1] = dg[1] - dl[1] * du[0];
+    du[1] = (du[1] - dl[1] * dw[0]) / dg[1];
+    dw[1] = dw[1] / dg[1];
+    for (int i = 2; i < m; ++i) {
+        dl[i] = dl[i] - ds[i] * du[i - 2];
+        dg[i] = dg[i] - ds[i] * dw[i - 2] - dl[i] * du[i - 1];
+        if (i < m - 2) dw[i] = dw[i] / dg[i];
+        if (i < m - 1) du[i] = (du[i] - dl[i] * dw[i - 1]) / dg[i];
+    }
+    auto solve = [&](double* x) {
         x[0] = x[0] / dg[0];
         x[1] = (x[1] - dl[1] * x[0]) / dg[1];
         for (int i = 2; i < m; ++i) x[i] = (x[i] - ds[i] * x[i - 2] - dl[i] * x[i - 1]) / dg[i];
@@ -405,7 +404,7 @@ static std::vector<double> build_table(int n, double lx, double gamma, double dt
         for (int i = m - 3; i >= 0; --i) x[i] = x[i] - du[i] * x[i + 1] - dw[i] * x[i + 2];
     };
     // border columns and omega (BatchHyper.cu:421-514)
-    std::vector<double> inv1(m, 0.0), inv2(m, 0.0);
+    for (int i = 0; i < m; ++i) inv1[i] = inv2[i] = 0.0;
     inv1[0] = a; inv1[m - 2] = e; inv1[m - 1] = d;
     inv2[0] = b; inv2[1] = a; inv2[m - 1] = e;
     solve(inv1);
@@ -416,7 +415,7 @@ static std::vector<double> build_table(int n, double lx, double gamma, double dt
     const double z22 = d * inv2[0] + e * inv2[1] + a * inv2[m - 1];
     const double y11 = c - z11, y12 = d - z12, y21 = b - z21, y22 = c - z22;
     const double det = 1.0 / (y11 * y22 - y21 * y12);
-    std::vector<double> t(tab_size(n), 0.0);
+    for (int k = 0; k < tab_size(n); ++k) t[k] = 0.0;
     for (int i = 0; i < m; ++i) {
         t[i] = (i > 1) ? ds[i] : 0.0;
         t[m + i] = (i > 0) ? dl[i] : 0.0;
@@ -437,6 +436,11 @@ static std::vector<double> build_table(int n, double lx, double gamma, double dt
     const double snl = (dt / 3.0) * D * (2.0 / (dx * dx));
     for (int k = 0; k < 25; ++k) t[7 * m + 8 + k] = wl[k] * sl;
     for (int k = 0; k < 9; ++k) t[7 * m + 33 + k] = wn[k] * snl;
+}
+
+static std::vector<double> build_table(int n, double lx, double gamma, double dt_factor) {
+    std::vector<double> t(tab_size(n)), work(7 * (n - 2));
+    fill_table(t.data(), work.data(), n, lx, gamma, dt_factor);
     return t;
 }
 
@@ -512,6 +516,36 @@ static int capture_pairs(Batch* b) {
     }
     return 0;
 }
+
+// ------------------------------------------------------------------------------------------------
+// Allocation-free single-grid step (custen_ch_step_noalloc)
+// ------------------------------------------------------------------------------------------------
+// Some callers cannot allocate device memory at all: a plug-in running inside a host application
+// that owns every device allocation through its own budgeted pool, or a latency-critical loop that
+// must never enter cudaMalloc / cudaFree (they synchronise the device). For them one step of one
+// grid runs with all of its work buffers in this file-scope array: the right-hand side / x-sweep
+// field, the row ends, the solver table, the descriptor, the work lists and the work counters.
+// Maximum grid: kNoAllocMaxN x kNoAllocMaxN. Every GPU that loads the library holds the array
+// (about 532 KiB) until the process exits.
+constexpr int kNoAllocMaxN = 256;
+constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+constexpr size_t kNoAllocTmpOff = 0;
+constexpr size_t kNoAllocEndsOff = align256(kNoAllocTmpOff + sizeof(double) * kNoAllocMaxN * kNoAllocMaxN);
+constexpr size_t kNoAllocTabOff = align256(kNoAllocEndsOff + sizeof(double) * 2 * kNoAllocMaxN);
+constexpr int kNoAllocTabLen = 7 * (kNoAllocMaxN - 2) + 42;
+constexpr size_t kNoAllocGridOff = align256(kNoAllocTabOff + sizeof(double) * kNoAllocTabLen);
+constexpr int kNoAllocBlocks = (kNoAllocMaxN / BLK) * (kNoAllocMaxN / BLK);
+constexpr int kNoAllocRows = kNoAllocMaxN / BLK;
+constexpr size_t kNoAllocRhsOff = align256(kNoAllocGridOff + sizeof(GridDev));
+constexpr size_t kNoAllocRowsOff = align256(kNoAllocRhsOff + sizeof(Item) * kNoAllocBlocks);
+constexpr size_t kNoAllocCtrOff = align256(kNoAllocRowsOff + sizeof(Item) * kNoAllocRows);
+constexpr size_t kNoAllocBytes = align256(kNoAllocCtrOff + 4 * sizeof(unsigned int));
+
+static __device__ __align__(256) unsigned char g_ch_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the array for each device, taken once with that device current. In host code the
+// array's name is only a host-side stand-in, never a device address.
+static unsigned char* g_noalloc_base[64] = {};
 
 }  // namespace ch
 }  // namespace custen
@@ -680,6 +714,77 @@ int custen_ch_batch_mean(void* h, int sim, double* mean) {
 }
 
 unsigned long long custen_ch_batch_launches(void* h) { return static_cast<Batch*>(h)->launches; }
+
+// One step of one n x n grid (n a multiple of 32, 64 <= n <= 256) without any device allocation.
+// c_old, c_cur: the two previous fields; c_new receives the next one (it may be the c_old buffer,
+// not the c_cur buffer). All three are device-accessible n*n double arrays. The first call on a
+// device looks up the scratch array's device address (make it before any stream capture). Calls
+// share the array: two calls that overlap on the GPU (different streams, no ordering) race.
+int custen_ch_step_noalloc(const double* c_old, const double* c_cur, double* c_new, int n, double lx, double gamma,
+                           double dt_factor, void* stream) {
+    if (!c_old || !c_cur || !c_new) return ch_fail_arg("custen_ch_step_noalloc: NULL field pointer");
+    if (n < 64 || n % BLK != 0) return ch_fail_arg("custen_ch_step_noalloc: n must be a multiple of 32, at least 64");
+    if (n > kNoAllocMaxN) {
+        char msg[160];
+        snprintf(msg, sizeof(msg), "custen_ch_step_noalloc: n = %d exceeds the allocation-free maximum of %d", n,
+                 kNoAllocMaxN);
+        return ch_fail_arg(msg);
+    }
+    if (c_new == c_cur) return ch_fail_arg("custen_ch_step_noalloc: c_new must not be the c_cur buffer");
+    int dev = 0;
+    CH_TRY(cudaGetDevice(&dev), "Querying the current device");
+    if (dev < 0 || dev >= 64) return ch_fail_arg("custen_ch_step_noalloc: device index out of range");
+    if (g_noalloc_base[dev] == nullptr) {
+        void* p = nullptr;
+        CH_TRY(cudaGetSymbolAddress(&p, g_ch_noalloc_scratch), "Looking up the scratch array's device address");
+        g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+    }
+    unsigned char* base = g_noalloc_base[dev];
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    // host-side inputs in stack buffers (no heap either)
+    double tab[kNoAllocTabLen];
+    double work[7 * (kNoAllocMaxN - 2)];
+    fill_table(tab, work, n, lx, gamma, dt_factor);
+    GridDev g{};
+    g.buf[0] = const_cast<double*>(c_cur);
+    g.buf[1] = c_new;
+    g.tmp = reinterpret_cast<double*>(base + kNoAllocTmpOff);
+    g.ends = reinterpret_cast<double*>(base + kNoAllocEndsOff);
+    g.tab = reinterpret_cast<const double*>(base + kNoAllocTabOff);
+    g.n = n;
+    const int bpr = n / BLK;
+    Item rhs[kNoAllocBlocks], rows[kNoAllocRows];
+    for (int k = 0; k < bpr * bpr; ++k) rhs[k] = Item{0, k};
+    for (int k = 0; k < bpr; ++k) rows[k] = Item{0, k};
+
+    const size_t bytes = (size_t)n * n * sizeof(double);
+    // the update is written over the "old" buffer: start it from c_old
+    if (c_new != c_old) CH_TRY(cudaMemcpyAsync(c_new, c_old, bytes, cudaMemcpyDefault, s), "Copying c_old");
+    CH_TRY(cudaMemcpyAsync(base + kNoAllocTabOff, tab, sizeof(double) * tab_size(n), cudaMemcpyHostToDevice, s),
+           "Uploading the solver table");
+    CH_TRY(cudaMemcpyAsync(base + kNoAllocGridOff, &g, sizeof(g), cudaMemcpyHostToDevice, s),
+           "Uploading the grid descriptor");
+    CH_TRY(cudaMemcpyAsync(base + kNoAllocRhsOff, rhs, sizeof(Item) * bpr * bpr, cudaMemcpyHostToDevice, s),
+           "Uploading the work list");
+    CH_TRY(cudaMemcpyAsync(base + kNoAllocRowsOff, rows, sizeof(Item) * bpr, cudaMemcpyHostToDevice, s),
+           "Uploading the work list");
+    // the work counters must start at zero on every call (the array keeps the previous call's values)
+    unsigned int* ctr = reinterpret_cast<unsigned int*>(base + kNoAllocCtrOff);
+    CH_TRY(cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned int), s), "Clearing the work counters");
+    const GridDev* gd = reinterpret_cast<const GridDev*>(base + kNoAllocGridOff);
+    const Item* it_rhs = reinterpret_cast<const Item*>(base + kNoAllocRhsOff);
+    const Item* it_rows = reinterpret_cast<const Item*>(base + kNoAllocRowsOff);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ch_rhs_kernel<double><<<std::min(bpr * bpr, sms * 16), BLK, 0, s>>>(gd, it_rhs, bpr * bpr, 0, ctr);
+    CH_TRY(cudaGetLastError(), "Launching right-hand side");
+    ch_xsolve_kernel<<<bpr, BLK, 0, s>>>(gd, it_rows, bpr, ctr + 1);
+    CH_TRY(cudaGetLastError(), "Launching x sweep");
+    ch_ysolve_kernel<<<bpr, BLK, 0, s>>>(gd, it_rows, bpr, 0, ctr + 2);
+    CH_TRY(cudaGetLastError(), "Launching y sweep");
+    return 0;
+}
 
 int custen_ch_batch_destroy(void* h) {
     Batch* b = static_cast<Batch*>(h);

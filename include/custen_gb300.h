@@ -141,6 +141,18 @@ int custen_ch_batch_mean(void* batch, int sim, double* mean);     /* compensated
 unsigned long long custen_ch_batch_launches(void* batch);
 int custen_ch_batch_destroy(void* batch);
 
+/* One Cahn-Hilliard step of one n x n grid that allocates nothing: for callers that cannot allocate
+ * device memory (a plug-in inside an application that owns all device memory, or a loop that must
+ * never enter cudaMalloc / cudaFree, which synchronise the device). Its work buffers live in a
+ * library-owned static device array sized for n <= 256 (about 532 KiB, held by every GPU that loads
+ * the library until exit); larger n is rejected with status 2. c_old and c_cur are the previous two
+ * fields, c_new receives the next (it may be the c_old buffer, not the c_cur buffer); all three are
+ * device-accessible n*n doubles. The first call on a device looks up the array's device address, so
+ * make it before any stream capture. Calls share the array: calls that overlap on the GPU race.
+ * No counterpart in the reference. */
+int custen_ch_step_noalloc(const double* c_old, const double* c_cur, double* c_new, int n, double lx, double gamma,
+                           double dt_factor, void* stream);
+
 /* ---- memory helpers for hosts without a CUDA runtime binding ---- */
 int custen_malloc_managed(void** ptr, size_t bytes);
 int custen_malloc_device(void** ptr, size_t bytes);
