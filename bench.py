@@ -352,6 +352,14 @@ def run_gpu(args, world, rank, local):
 
     for h in hs64:
         h.destroy()
+    del inp64, outs64, keep64
+    torch.cuda.synchronize(dev)
+    torch.cuda.empty_cache()
+
+    ch_batched = ch_served = None
+    if not args.skip_ch:
+        ch_batched = run_ch_batched(args, cs)
+        ch_served = run_ch_served(args, cs)
 
     if rank == 0:
         line = {
@@ -380,6 +388,9 @@ def run_gpu(args, world, rank, local):
             line["e2e"] = e2e
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if ch_batched is not None:
+            line["ch_batched"] = ch_batched
+            line["ch_served"] = ch_served
         print(json.dumps(line), flush=True)
     if pg:
         pg.barrier()
@@ -435,6 +446,106 @@ def run_e2e(args, cs, np, local, ops):
             "path": f"managed host buffers {n}^2, numTiles=4, Compute(HOST) per operator (tile streaming)"}
 
 
+# ----------------------------------------------------------------------------------------------
+# Cahn-Hilliard ADI: batched (config 4) and served (config 5)
+# ----------------------------------------------------------------------------------------------
+def plain_step_seconds(cs, n: int, steps: int = 10) -> float:
+    """One grid at a time, one step per launch sequence with a synchronisation after every step (the
+    structure of the reference's plain loop, cuPentCahnADI.cu:528-596), timed per step."""
+    import numpy as np
+    b = cs.CahnHilliardBatch([n])
+    b.set_state(0, np.random.default_rng(n).uniform(-0.1, 0.1, (n, n)))
+    b.step(2, graph=False)
+    b.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b.step(1, graph=False)
+        b.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    b.close()
+    return dt
+
+
+def run_ch_batched(args, cs):
+    """512 periodic grids, N uniform over {64,...,1024} (seed 2), c0 ~ U(-0.1, 0.1), 500 steps."""
+    import numpy as np
+    rng = np.random.default_rng(2)
+    sizes = [int(v) for v in rng.choice([64, 128, 256, 512, 1024], size=args.ch_sims)]
+    steps = args.ch_steps
+    out = {"config": f"{args.ch_sims} grids, N uniform over {{64..1024}} (seed 2), {steps} steps, lx = 2 pi, "
+                     f"gamma 0.01, dt = 0.1 dx", "points": int(sum(n * n for n in sizes))}
+    for label, dt in (("fp64", cs.F64), ("fp32_stencil", cs.F32)):
+        b = cs.CahnHilliardBatch(sizes, rhs_dtype=dt)
+        crng = np.random.default_rng(3)
+        for k, n in enumerate(sizes):
+            b.set_state(k, crng.uniform(-0.1, 0.1, (n, n)))
+        b.step(2)
+        b.synchronize()
+        l0 = b.launches()
+        t0 = time.perf_counter()
+        b.step(steps)
+        b.synchronize()
+        wall = time.perf_counter() - t0
+        out[label] = {"wall_s": round(wall, 4), "steps_per_s": round(len(sizes) * steps / wall, 1),
+                      "gpt_steps_per_s": round(out["points"] * steps / wall / 1e9, 3),
+                      "ms_per_step": round(wall / steps * 1e3, 4), "launches": b.launches() - l0,
+                      "graphs": "pairs of steps"}
+        b.close()
+    # plain loop on the same GPU: one grid at a time (per-size step time measured, then summed)
+    per_size = {n: plain_step_seconds(cs, n) for n in sorted(set(sizes))}
+    plain_total = sum(per_size[n] * steps for n in sizes)
+    out["plain_loop"] = {"steps_per_s": round(len(sizes) * steps / plain_total, 1),
+                         "wall_s_estimated": round(plain_total, 3),
+                         "step_ms_by_n": {str(n): round(v * 1e3, 4) for n, v in per_size.items()},
+                         "method": "this library's kernels, one grid per launch sequence, synchronised per "
+                                   "step; per-size step time x steps, summed over grids"}
+    out["speedup_vs_plain_loop"] = round(out["fp64"]["steps_per_s"] / out["plain_loop"]["steps_per_s"], 2)
+    return out
+
+
+def run_ch_served(args, cs):
+    """Poisson arrivals (mean rate, seed 3), N log-uniform 128-2048 rounded to 32, steps U(100, 5000),
+    c0 ~ U(-0.1, 0.1), HBM budget 150 GB, a fixed number of requests."""
+    import numpy as np
+    rng = np.random.default_rng(3)
+    R = args.served_requests
+    gaps = rng.exponential(1.0 / args.served_rate, size=R)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    sizes = [int(max(128, min(2048, round(math.exp(v) / 32) * 32)))
+             for v in rng.uniform(math.log(128), math.log(2048), size=R)]
+    steps = [int(v) for v in rng.integers(100, 5001, size=R)]
+    srv = cs.CahnHilliardServer(hbm_budget_bytes=150e9, chunk_steps=args.served_chunk, keep_results=False)
+    for k in range(R):
+        srv.submit(sizes[k], steps[k], arrival=float(arrivals[k]), seed=1000 + k)
+    srv.run()
+    st = srv.stats()
+    ttc = np.array([srv.result(k, field=False)["ttc"] for k in range(R)])
+    drift = max(abs(srv.result(k, field=False)["mean_end"] - srv.result(k, field=False)["mean0"]) for k in range(R))
+    srv.close()
+    total_steps = int(sum(steps))
+    out = {"config": f"{R} requests, Poisson {args.served_rate}/s (seed 3), N log-uniform 128-2048 (multiples of "
+                     f"32), steps U(100, 5000), budget 150 GB, chunk {args.served_chunk} steps",
+           "makespan_s": round(st["makespan"], 3), "steps_per_s": round(total_steps / st["makespan"], 1),
+           "gpt_steps_per_s": round(st["point_steps"] / st["makespan"] / 1e9, 3),
+           "ttc_p50_s": round(float(np.percentile(ttc, 50)), 3), "ttc_p99_s": round(float(np.percentile(ttc, 99)), 3),
+           "max_resident": st["max_active"], "peak_resident_gb": round(st["peak_bytes"] / 1e9, 2),
+           "max_mass_drift": drift}
+    # the plain sequential loop: first come first served, one grid at a time
+    per_size = {n: plain_step_seconds(cs, n, steps=5) for n in sorted(set(sizes))}
+    t = 0.0
+    ttc_p = []
+    for k in range(R):
+        start = max(t, float(arrivals[k]))
+        t = start + steps[k] * per_size[sizes[k]]
+        ttc_p.append(t - float(arrivals[k]))
+    out["plain_loop"] = {"makespan_s": round(t, 3), "steps_per_s": round(total_steps / t, 1),
+                         "ttc_p50_s": round(float(np.percentile(ttc_p, 50)), 3),
+                         "ttc_p99_s": round(float(np.percentile(ttc_p, 99)), 3),
+                         "method": "FCFS queue over the measured per-size step time of one grid at a time"}
+    out["speedup_vs_plain_loop"] = round(out["steps_per_s"] / out["plain_loop"]["steps_per_s"], 2)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -448,6 +559,12 @@ def main():
     ap.add_argument("--skip-fp32", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-ch", action="store_true")
+    ap.add_argument("--ch-sims", type=int, default=512)
+    ap.add_argument("--ch-steps", type=int, default=500)
+    ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--served-rate", type=float, default=200.0)
+    ap.add_argument("--served-chunk", type=int, default=16)
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch from an ncu capture (recorded in the roofline object)")
     args = ap.parse_args()

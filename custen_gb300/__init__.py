@@ -79,6 +79,15 @@ def lib() -> ctypes.CDLL:
         L.custen_ch_batch_launches.argtypes = [vp]
         L.custen_ch_batch_launches.restype = ull
         L.custen_ch_batch_destroy.argtypes = [vp]
+        L.custen_ch_server_last_error.restype = ctypes.c_char_p
+        L.custen_ch_server_create.argtypes = [ctypes.POINTER(vp), ctypes.c_double, i, ctypes.c_double, ctypes.c_double,
+                                              i, i]
+        L.custen_ch_server_submit.argtypes = [vp, i, ctypes.c_double, i, vp, ull, ctypes.c_double, ctypes.POINTER(i)]
+        L.custen_ch_server_run.argtypes = [vp]
+        L.custen_ch_server_result.argtypes = [vp, i, vp, dp, dp, dp, dp, dp]
+        L.custen_ch_server_stats.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), dp, ctypes.POINTER(i), dp,
+                                             ctypes.POINTER(ull)]
+        L.custen_ch_server_destroy.argtypes = [vp]
         L.custen_ch_step_noalloc.argtypes = [vp, vp, vp, i, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
         _lib = L
     return _lib
@@ -275,6 +284,67 @@ class CahnHilliardBatch:
     def close(self) -> None:
         if self.h:
             lib().custen_ch_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _srv_check(status: int) -> None:
+    if status != 0:
+        raise CustenError(lib().custen_ch_server_last_error().decode(errors="replace"))
+
+
+class CahnHilliardServer:
+    """Request loop with continuous batching of Cahn-Hilliard simulations (include/custen_gb300.h)."""
+
+    def __init__(self, hbm_budget_bytes: float = 150e9, rhs_dtype: int = F64, gamma: float = 0.01,
+                 dt_factor: float = 0.1, chunk_steps: int = 8, keep_results: bool = True):
+        h = ctypes.c_void_p()
+        _srv_check(lib().custen_ch_server_create(ctypes.byref(h), hbm_budget_bytes, rhs_dtype, gamma, dt_factor,
+                                                 chunk_steps, int(keep_results)))
+        self.h = h.value
+        self.sizes = []
+
+    def submit(self, n: int, steps: int, arrival: float = 0.0, c0=None, seed: int = 0, lx: float = 0.0) -> int:
+        import numpy as np
+        rid = ctypes.c_int()
+        ptr = None
+        if c0 is not None:
+            c0 = np.ascontiguousarray(c0, dtype=np.float64)
+            ptr = c0.ctypes.data
+        _srv_check(lib().custen_ch_server_submit(self.h, n, lx, steps, ptr, seed, arrival, ctypes.byref(rid)))
+        self.sizes.append(n)
+        return rid.value
+
+    def run(self) -> None:
+        _srv_check(lib().custen_ch_server_run(self.h))
+
+    def result(self, rid: int, field: bool = True):
+        import numpy as np
+        n = self.sizes[rid]
+        out = np.empty((n, n)) if field else None
+        vals = [ctypes.c_double() for _ in range(5)]
+        _srv_check(lib().custen_ch_server_result(self.h, rid, None if out is None else out.ctypes.data,
+                                                 *[ctypes.byref(v) for v in vals]))
+        arrival, admit, done, m0, m1 = (v.value for v in vals)
+        return {"field": out, "arrival": arrival, "admit": admit, "done": done, "mean0": m0, "mean_end": m1,
+                "ttc": done - arrival}
+
+    def stats(self):
+        mk, pts, bts = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        st, ma, la = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_ulonglong()
+        _srv_check(lib().custen_ch_server_stats(self.h, ctypes.byref(mk), ctypes.byref(st), ctypes.byref(pts),
+                                                ctypes.byref(ma), ctypes.byref(bts), ctypes.byref(la)))
+        return {"makespan": mk.value, "steps": st.value, "point_steps": pts.value, "max_active": ma.value,
+                "peak_bytes": bts.value, "launches": la.value}
+
+    def close(self):
+        if self.h:
+            lib().custen_ch_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

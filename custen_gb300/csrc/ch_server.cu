@@ -1,0 +1,436 @@
+// Cahn-Hilliard serving: a request loop with continuous batching over resident simulations.
+//
+// Requests (grid size n, step count, initial field, arrival time) arrive over time. The loop admits
+// arrived requests first-come first-served while their device memory fits the HBM budget: their two
+// field buffers, work field and row ends are allocated stream-ordered (cudaMallocAsync, no device
+// synchronisation) and their pre-factored solver table is shared by every resident grid of the same
+// size. All resident grids then advance together, a chunk of steps at a time, through the same
+// persistent kernels as the batch solver (ch_solver.cu): one launch per kernel covers every grid.
+// Between chunks, finished grids are read back and their memory is released, and new arrivals join,
+// so work that arrives while others are on the GPU overlaps with them. Each grid is computed by the
+// same operations whatever else is resident, so a result is bit-identical alone and in the mix.
+//
+// The solver is the reference's (cuPentCahnADI/src/cuPentCahnADI.cu:197-627); the request loop has
+// no counterpart in the reference, whose driver runs one simulation per process.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/custen_gb300.h"
+#include "ch_internal.cuh"
+
+namespace custen {
+namespace ch {
+
+// Counter-based uniform initial field U(lo, hi) from a seed (splitmix64 of seed and index).
+__global__ void ch_fill_uniform_kernel(double* f, long long count, unsigned long long seed, double lo, double hi) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count;
+         k += (long long)gridDim.x * blockDim.x) {
+        unsigned long long z = seed * 0x9E3779B97F4A7C15ull + (unsigned long long)k + 1ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);   // [0, 1)
+        f[k] = lo + u * (hi - lo);
+    }
+}
+
+struct Request {
+    int n = 0;
+    double lx = 0.0;
+    int steps = 0;
+    double arrival = 0.0;            // seconds on the server clock
+    std::vector<double> c0;          // host initial field (empty: generated on the device from seed)
+    unsigned long long seed = 0;
+    int state = 0;                   // 0 pending, 1 resident, 2 done
+    int remaining = 0;
+    double admit_t = -1.0, done_t = -1.0;
+    double mean0 = 0.0, mean_end = 0.0;
+    std::vector<double> result;
+    size_t bytes = 0;
+    GridDev g{};
+    std::string table_key;
+};
+
+struct TableRef {
+    double* ptr = nullptr;
+    int refs = 0;
+    size_t bytes = 0;
+};
+
+struct Server {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int rhs_fp32 = 0;
+    double gamma = 0.01, dt_factor = 0.1;
+    double budget = 0.0;
+    double used = 0.0;
+    int chunk = 8;
+    int keep_results = 1;
+    int parity = 0;
+    std::vector<Request> reqs;
+    std::vector<int> active;        // request ids resident on the device
+    std::map<std::string, TableRef> tables;
+    GridDev* grids_d = nullptr;
+    Item* items_rhs_d = nullptr;
+    Item* items_rows_d = nullptr;
+    size_t cap_grids = 0, cap_rhs = 0, cap_rows = 0;
+    int n_rhs = 0, n_rows = 0;
+    unsigned int* counters = nullptr;
+    double* mass_d = nullptr;
+    int sms = 0;
+    // statistics of the last run
+    double makespan = 0.0;
+    long long total_steps = 0;
+    double total_pt_steps = 0.0;
+    int max_active = 0;
+    double max_used = 0.0;
+    unsigned long long launches = 0;
+};
+
+static thread_local std::string g_srv_err;
+static int srv_fail(cudaError_t e, const char* what) {
+    g_srv_err = std::string("Error while '") + what + "': " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return 1;
+}
+static int srv_arg(const std::string& m) {
+    g_srv_err = m;
+    return 2;
+}
+#define SRV_TRY(x, what)                                \
+    do {                                                \
+        cudaError_t _e = (x);                           \
+        if (_e != cudaSuccess) return srv_fail(_e, what); \
+    } while (0)
+
+static size_t grid_bytes(int n) { return 3 * (size_t)n * n * sizeof(double) + 2 * (size_t)n * sizeof(double); }
+
+static int grow(void** p, size_t* cap, size_t need, size_t elem, cudaStream_t s) {
+    if (need <= *cap) return 0;
+    size_t nc = std::max(need, *cap * 2 + 16);
+    if (*p) SRV_TRY(cudaFreeAsync(*p, s), "Releasing a work list");
+    SRV_TRY(cudaMallocAsync(p, nc * elem, s), "Allocating a work list");
+    *cap = nc;
+    return 0;
+}
+
+// Rebuild the device work lists of the resident grids (largest first).
+static int rebuild(Server* S) {
+    std::vector<int> order = S->active;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return S->reqs[a].n > S->reqs[b].n; });
+    std::vector<GridDev> grids;
+    std::vector<Item> rhs, rows;
+    for (size_t k = 0; k < order.size(); ++k) {
+        const Request& r = S->reqs[order[k]];
+        grids.push_back(r.g);
+        const int bpr = r.n / BLK;
+        for (int b = 0; b < bpr * bpr; ++b) rhs.push_back({(int)k, b});
+        for (int b = 0; b < bpr; ++b) rows.push_back({(int)k, b});
+    }
+    int st;
+    if ((st = grow((void**)&S->grids_d, &S->cap_grids, grids.size(), sizeof(GridDev), S->stream))) return st;
+    if ((st = grow((void**)&S->items_rhs_d, &S->cap_rhs, rhs.size(), sizeof(Item), S->stream))) return st;
+    if ((st = grow((void**)&S->items_rows_d, &S->cap_rows, rows.size(), sizeof(Item), S->stream))) return st;
+    // pageable copies: the host vectors may be released as soon as the calls return
+    SRV_TRY(cudaMemcpyAsync(S->grids_d, grids.data(), grids.size() * sizeof(GridDev), cudaMemcpyHostToDevice,
+                            S->stream), "Uploading grid descriptors");
+    SRV_TRY(cudaMemcpyAsync(S->items_rhs_d, rhs.data(), rhs.size() * sizeof(Item), cudaMemcpyHostToDevice, S->stream),
+            "Uploading work list");
+    SRV_TRY(cudaMemcpyAsync(S->items_rows_d, rows.data(), rows.size() * sizeof(Item), cudaMemcpyHostToDevice,
+                            S->stream), "Uploading work list");
+    S->n_rhs = (int)rhs.size();
+    S->n_rows = (int)rows.size();
+    return 0;
+}
+
+static int admit(Server* S, int id, double now) {
+    Request& r = S->reqs[id];
+    char key[128];
+    snprintf(key, sizeof(key), "%d/%.17g", r.n, r.lx);
+    r.table_key = key;
+    TableRef& t = S->tables[key];
+    if (!t.ptr) {
+        std::vector<double> h = build_table(r.n, r.lx, S->gamma, S->dt_factor);
+        t.bytes = h.size() * sizeof(double);
+        SRV_TRY(cudaMallocAsync(&t.ptr, t.bytes, S->stream), "Allocating a solver table");
+        SRV_TRY(cudaMemcpyAsync(t.ptr, h.data(), t.bytes, cudaMemcpyHostToDevice, S->stream), "Uploading a table");
+        S->used += (double)t.bytes;
+    }
+    ++t.refs;
+    const size_t f = (size_t)r.n * r.n * sizeof(double);
+    double* p[4];
+    for (int k = 0; k < 4; ++k)
+        SRV_TRY(cudaMallocAsync(&p[k], k < 3 ? f : 2 * (size_t)r.n * sizeof(double), S->stream), "Allocating a grid");
+    r.g.buf[S->parity] = p[0];        // cCurr
+    r.g.buf[S->parity ^ 1] = p[1];    // cOld
+    r.g.tmp = p[2];
+    r.g.ends = p[3];
+    r.g.tab = t.ptr;
+    r.g.n = r.n;
+    if (!r.c0.empty()) {
+        SRV_TRY(cudaMemcpyAsync(p[0], r.c0.data(), f, cudaMemcpyHostToDevice, S->stream), "Uploading c0");
+    } else {
+        const long long count = (long long)r.n * r.n;
+        ch_fill_uniform_kernel<<<std::min<long long>((count + 255) / 256, 4096), 256, 0, S->stream>>>(
+            p[0], count, r.seed, -0.1, 0.1);
+        SRV_TRY(cudaGetLastError(), "Generating c0");
+    }
+    SRV_TRY(cudaMemcpyAsync(p[1], p[0], f, cudaMemcpyDeviceToDevice, S->stream), "Copying c0");
+    ch_mass_kernel<<<1, 256, 0, S->stream>>>(p[0], (long long)r.n * r.n, S->mass_d);
+    double m = 0.0;
+    SRV_TRY(cudaMemcpyAsync(&m, S->mass_d, sizeof(double), cudaMemcpyDeviceToHost, S->stream), "Reading mass");
+    SRV_TRY(cudaStreamSynchronize(S->stream), "Admitting");
+    r.mean0 = m / ((double)r.n * r.n);
+    r.bytes = grid_bytes(r.n);
+    S->used += (double)r.bytes;
+    r.state = 1;
+    r.remaining = r.steps;
+    r.admit_t = now;
+    S->active.push_back(id);
+    return 0;
+}
+
+static int retire(Server* S, int id, double now_after) {
+    Request& r = S->reqs[id];
+    const double* cur = r.g.buf[S->parity];
+    ch_mass_kernel<<<1, 256, 0, S->stream>>>(cur, (long long)r.n * r.n, S->mass_d);
+    double m = 0.0;
+    SRV_TRY(cudaMemcpyAsync(&m, S->mass_d, sizeof(double), cudaMemcpyDeviceToHost, S->stream), "Reading mass");
+    if (S->keep_results) {
+        r.result.resize((size_t)r.n * r.n);
+        SRV_TRY(cudaMemcpyAsync(r.result.data(), cur, r.result.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                S->stream), "Reading a result");
+    }
+    SRV_TRY(cudaStreamSynchronize(S->stream), "Retiring");
+    r.mean_end = m / ((double)r.n * r.n);
+    r.done_t = now_after;
+    for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends}) SRV_TRY(cudaFreeAsync(p, S->stream), "Freeing a grid");
+    S->used -= (double)r.bytes;
+    TableRef& t = S->tables[r.table_key];
+    if (--t.refs == 0) {
+        SRV_TRY(cudaFreeAsync(t.ptr, S->stream), "Freeing a table");
+        S->used -= (double)t.bytes;
+        t.ptr = nullptr;
+    }
+    r.state = 2;
+    return 0;
+}
+
+static int enqueue_steps(Server* S, int k) {
+    for (int s = 0; s < k; ++s) {
+        SRV_TRY(cudaMemsetAsync(S->counters, 0, 3 * sizeof(unsigned int), S->stream), "Resetting counters");
+        const int g1 = std::min(S->n_rhs, S->sms * 16), g23 = std::min(S->n_rows, S->sms * 16);
+        if (S->rhs_fp32)
+            ch_rhs_kernel<float><<<g1, BLK, 0, S->stream>>>(S->grids_d, S->items_rhs_d, S->n_rhs, S->parity,
+                                                              S->counters);
+        else
+            ch_rhs_kernel<double><<<g1, BLK, 0, S->stream>>>(S->grids_d, S->items_rhs_d, S->n_rhs, S->parity,
+                                                               S->counters);
+        ch_xsolve_kernel<<<g23, BLK, 0, S->stream>>>(S->grids_d, S->items_rows_d, S->n_rows, S->counters + 1);
+        ch_ysolve_kernel<<<g23, BLK, 0, S->stream>>>(S->grids_d, S->items_rows_d, S->n_rows, S->parity,
+                                                       S->counters + 2);
+        SRV_TRY(cudaGetLastError(), "Launching a step");
+        S->launches += 3;
+        S->parity ^= 1;
+    }
+    return 0;
+}
+
+static int run(Server* S) {
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    auto now = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
+    std::vector<int> order(S->reqs.size());
+    for (size_t k = 0; k < order.size(); ++k) order[k] = (int)k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return S->reqs[a].arrival < S->reqs[b].arrival; });
+    size_t next = 0;   // first request (in arrival order) not yet admitted
+    S->total_steps = 0;
+    S->total_pt_steps = 0.0;
+    S->max_active = 0;
+    S->max_used = S->used;
+    int done = 0;
+    const int total = (int)S->reqs.size();
+    while (done < total) {
+        bool changed = false;
+        // admit arrived requests, first come first served, while their memory fits the budget
+        while (next < order.size()) {
+            Request& r = S->reqs[order[next]];
+            if (r.state != 0) { ++next; continue; }
+            if (r.arrival > now()) break;
+            const double need = (double)grid_bytes(r.n);
+            if (S->used + need > S->budget && !S->active.empty()) break;
+            int st = admit(S, order[next], now());
+            if (st) return st;
+            ++next;
+            changed = true;
+        }
+        if (S->active.empty()) {
+            if (next < order.size()) {
+                const double wait = S->reqs[order[next]].arrival - now();
+                if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.05)));
+            }
+            continue;
+        }
+        if (changed) {
+            int st = rebuild(S);
+            if (st) return st;
+        }
+        S->max_active = std::max<int>(S->max_active, (int)S->active.size());
+        S->max_used = std::max(S->max_used, S->used);
+        int k = S->chunk;
+        for (int id : S->active) k = std::min(k, S->reqs[id].remaining);
+        int st = enqueue_steps(S, k);
+        if (st) return st;
+        SRV_TRY(cudaStreamSynchronize(S->stream), "Running a chunk");
+        const double t_chunk = now();
+        std::vector<int> still;
+        bool retired = false;
+        for (int id : S->active) {
+            Request& r = S->reqs[id];
+            r.remaining -= k;
+            S->total_steps += k;
+            S->total_pt_steps += (double)k * r.n * r.n;
+            if (r.remaining == 0) {
+                st = retire(S, id, t_chunk);
+                if (st) return st;
+                ++done;
+                retired = true;
+            } else {
+                still.push_back(id);
+            }
+        }
+        S->active.swap(still);
+        if (retired && !S->active.empty()) {
+            st = rebuild(S);
+            if (st) return st;
+        }
+    }
+    S->makespan = now();
+    return 0;
+}
+
+}  // namespace ch
+}  // namespace custen
+
+using namespace custen::ch;
+
+extern "C" {
+
+const char* custen_ch_server_last_error(void) { return g_srv_err.c_str(); }
+
+int custen_ch_server_create(void** out, double hbm_budget_bytes, int rhs_dtype, double gamma, double dt_factor,
+                            int chunk_steps, int keep_results) {
+    if (!out || hbm_budget_bytes <= 0 || chunk_steps < 1) return srv_arg("invalid arguments");
+    Server* S = new Server();
+    cudaGetDevice(&S->device);
+    cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->device);
+    S->budget = hbm_budget_bytes;
+    S->rhs_fp32 = rhs_dtype == CUSTEN_F32;
+    S->gamma = gamma;
+    S->dt_factor = dt_factor;
+    S->chunk = chunk_steps;
+    S->keep_results = keep_results;
+    cudaError_t e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocAsync(&S->counters, 4 * sizeof(unsigned int), S->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&S->mass_d, sizeof(double), S->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+    if (e != cudaSuccess) {
+        delete S;
+        return srv_fail(e, "Creating the server");
+    }
+    *out = S;
+    return 0;
+}
+
+// Queue a request: an n x n grid of side lx advanced `steps` steps, arriving `arrival` seconds after
+// the start of the run. c0: host initial field (n*n doubles), or NULL to draw U(-0.1, 0.1) from seed.
+int custen_ch_server_submit(void* h, int n, double lx, int steps, const double* c0, unsigned long long seed,
+                            double arrival, int* req_id) {
+    Server* S = static_cast<Server*>(h);
+    if (!S || n < 64 || n % BLK != 0 || steps < 1) return srv_arg("invalid request (n: multiple of 32, >= 64)");
+    Request r;
+    r.n = n;
+    r.lx = lx > 0 ? lx : 2.0 * M_PI;
+    r.steps = steps;
+    r.arrival = arrival;
+    r.seed = seed;
+    if (c0) r.c0.assign(c0, c0 + (size_t)n * n);
+    S->reqs.push_back(std::move(r));
+    if (req_id) *req_id = (int)S->reqs.size() - 1;
+    return 0;
+}
+
+int custen_ch_server_run(void* h) {
+    Server* S = static_cast<Server*>(h);
+    if (!S) return srv_arg("invalid server");
+    cudaSetDevice(S->device);
+    return run(S);
+}
+
+// Per-request outcome: times on the server clock (seconds), means of the initial and final fields
+// (compensated sums), and the final field when results are kept (c_out may be NULL).
+int custen_ch_server_result(void* h, int id, double* c_out, double* arrival, double* admit_t, double* done_t,
+                            double* mean0, double* mean_end) {
+    Server* S = static_cast<Server*>(h);
+    if (!S || id < 0 || id >= (int)S->reqs.size()) return srv_arg("invalid request id");
+    const Request& r = S->reqs[id];
+    if (r.state != 2) return srv_arg("request not completed");
+    if (c_out) {
+        if (r.result.empty()) return srv_arg("results were not kept");
+        memcpy(c_out, r.result.data(), r.result.size() * sizeof(double));
+    }
+    if (arrival) *arrival = r.arrival;
+    if (admit_t) *admit_t = r.admit_t;
+    if (done_t) *done_t = r.done_t;
+    if (mean0) *mean0 = r.mean0;
+    if (mean_end) *mean_end = r.mean_end;
+    return 0;
+}
+
+// stats: makespan (s), total steps, total point-steps, largest resident set, peak resident bytes,
+// kernel launches.
+int custen_ch_server_stats(void* h, double* makespan, long long* total_steps, double* total_pt_steps, int* max_active,
+                           double* peak_bytes, unsigned long long* launches) {
+    Server* S = static_cast<Server*>(h);
+    if (!S) return srv_arg("invalid server");
+    if (makespan) *makespan = S->makespan;
+    if (total_steps) *total_steps = S->total_steps;
+    if (total_pt_steps) *total_pt_steps = S->total_pt_steps;
+    if (max_active) *max_active = S->max_active;
+    if (peak_bytes) *peak_bytes = S->max_used;
+    if (launches) *launches = S->launches;
+    return 0;
+}
+
+int custen_ch_server_destroy(void* h) {
+    Server* S = static_cast<Server*>(h);
+    if (!S) return 0;
+    cudaStreamSynchronize(S->stream);
+    for (int id : S->active) {
+        Request& r = S->reqs[id];
+        for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends}) cudaFreeAsync(p, S->stream);
+    }
+    for (auto& t : S->tables)
+        if (t.second.ptr) cudaFreeAsync(t.second.ptr, S->stream);
+    if (S->grids_d) cudaFreeAsync(S->grids_d, S->stream);
+    if (S->items_rhs_d) cudaFreeAsync(S->items_rhs_d, S->stream);
+    if (S->items_rows_d) cudaFreeAsync(S->items_rows_d, S->stream);
+    cudaFreeAsync(S->counters, S->stream);
+    cudaFreeAsync(S->mass_d, S->stream);
+    cudaStreamSynchronize(S->stream);
+    cudaStreamDestroy(S->stream);
+    delete S;
+    return 0;
+}
+
+}  // extern "C"

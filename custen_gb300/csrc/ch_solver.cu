@@ -33,34 +33,10 @@
 #include <vector>
 
 #include "../../include/custen_gb300.h"
+#include "ch_internal.cuh"
 
 namespace custen {
 namespace ch {
-
-constexpr int BLK = 32;   // rows / columns per work item; n must be a multiple of 32
-
-// Per-grid descriptor (device).
-struct GridDev {
-    double* buf[2];       // the two field buffers: cCurr = buf[parity], cOld = buf[parity ^ 1]
-    double* tmp;          // n x n work field (rhs, then the x-sweep solution)
-    double* ends;         // 2 n values: the x sweep's last two unknowns of every row
-    const double* tab;    // solver table for n (layout below)
-    int n;
-    int pad;
-};
-
-// Table layout for one n (m = n - 2), all double:
-//   [0, m) ds  [m, 2m) dl  [2m, 3m) rd = 1/diag  [3m, 4m) du  [4m, 5m) dw   (factored, zero-padded:
-//   ds[0] = ds[1] = dl[0] = 0, du[m-1] = 0, dw[m-2] = dw[m-1] = 0)
-//   [5m, 6m) inv1  [6m, 7m) inv2   border columns of the cyclic correction
-//   [7m, 7m+4) omega  [7m+4, 7m+8) a, b, d, e  [7m+8, 7m+33) linear 5x5 weights  [7m+33, 7m+42) the
-//   non-linear 3x3 weights
-__host__ __device__ inline int tab_size(int n) { return 7 * (n - 2) + 42; }
-
-struct Item {
-    int grid;
-    int block;   // K1: 32 x 32 block index (row-major over the grid); K2: row block; K3: column block
-};
 
 // ------------------------------------------------------------------------------------------------
 // K1: right-hand side
@@ -438,7 +414,7 @@ static void fill_table(double* t, double* work, int n, double lx, double gamma, 
     for (int k = 0; k < 9; ++k) t[7 * m + 33 + k] = wn[k] * snl;
 }
 
-static std::vector<double> build_table(int n, double lx, double gamma, double dt_factor) {
+std::vector<double> build_table(int n, double lx, double gamma, double dt_factor) {
     std::vector<double> t(tab_size(n)), work(7 * (n - 2));
     fill_table(t.data(), work.data(), n, lx, gamma, dt_factor);
     return t;
@@ -805,3 +781,11 @@ int custen_ch_batch_destroy(void* h) {
 }
 
 }  // extern "C"
+
+// Explicit instantiations for the other host translation units (the server).
+template __global__ void custen::ch::ch_rhs_kernel<double>(const custen::ch::GridDev* __restrict__,
+                                                           const custen::ch::Item* __restrict__, int, int,
+                                                           unsigned int*);
+template __global__ void custen::ch::ch_rhs_kernel<float>(const custen::ch::GridDev* __restrict__,
+                                                          const custen::ch::Item* __restrict__, int, int,
+                                                          unsigned int*);

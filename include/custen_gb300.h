@@ -141,6 +141,24 @@ int custen_ch_batch_mean(void* batch, int sim, double* mean);     /* compensated
 unsigned long long custen_ch_batch_launches(void* batch);
 int custen_ch_batch_destroy(void* batch);
 
+/* ---- Cahn-Hilliard serving: request loop with continuous batching ----
+ * Requests (n, steps, c0 or a seed for c0 ~ U(-0.1, 0.1), arrival time) are queued, then run()
+ * admits arrived requests first-come first-served within the HBM budget, advances every resident
+ * grid together a chunk of steps at a time (one launch per kernel for all grids), retires finished
+ * grids and admits new arrivals between chunks. Times are seconds on the server clock of run().
+ * No counterpart in the reference (its driver runs one simulation per process). */
+const char* custen_ch_server_last_error(void);
+int custen_ch_server_create(void** server, double hbm_budget_bytes, int rhs_dtype, double gamma, double dt_factor,
+                            int chunk_steps, int keep_results);
+int custen_ch_server_submit(void* server, int n, double lx, int steps, const double* c0, unsigned long long seed,
+                            double arrival, int* request_id);
+int custen_ch_server_run(void* server);
+int custen_ch_server_result(void* server, int request_id, double* c_out, double* arrival, double* admit_t,
+                            double* done_t, double* mean0, double* mean_end);
+int custen_ch_server_stats(void* server, double* makespan, long long* total_steps, double* total_point_steps,
+                           int* max_active, double* peak_bytes, unsigned long long* launches);
+int custen_ch_server_destroy(void* server);
+
 /* One Cahn-Hilliard step of one n x n grid that allocates nothing: for callers that cannot allocate
  * device memory (a plug-in inside an application that owns all device memory, or a loop that must
  * never enter cudaMalloc / cudaFree, which synchronise the device). Its work buffers live in a
