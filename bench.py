@@ -359,7 +359,7 @@ def run_gpu(args, world, rank, local):
     ch_batched = ch_served = None
     if not args.skip_ch:
         ch_batched = run_ch_batched(args, cs)
-        ch_served = run_ch_served(args, cs)
+        ch_served = None if args.skip_served else run_ch_served(args, cs)
 
     if rank == 0:
         line = {
@@ -390,7 +390,8 @@ def run_gpu(args, world, rank, local):
             line["cpu_baseline"] = cpu
         if ch_batched is not None:
             line["ch_batched"] = ch_batched
-            line["ch_served"] = ch_served
+            if ch_served is not None:
+                line["ch_served"] = ch_served
         print(json.dumps(line), flush=True)
     if pg:
         pg.barrier()
@@ -560,6 +561,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-ch", action="store_true")
+    ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--ch-sims", type=int, default=512)
     ap.add_argument("--ch-steps", type=int, default=500)
     ap.add_argument("--served-requests", type=int, default=48)
