@@ -129,12 +129,17 @@ __global__ void __launch_bounds__(BLK) ch_rhs_kernel(const GridDev* __restrict__
 // ------------------------------------------------------------------------------------------------
 // K2: x sweep (lane = row), 32-column chunks through shared memory
 // ------------------------------------------------------------------------------------------------
+// The recurrences are latency chains of FP64 operations; everything else is taken off their path:
+// the 32 solver-table entries of a chunk are loaded once, coalesced (lane k holds entry k), and
+// broadcast with shuffles as the chain walks the chunk, and a chunk's 32 x 32 field values are all
+// in flight before the chain starts.
 __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restrict__ grids,
                                                         const Item* __restrict__ items, int n_items,
                                                         unsigned int* counter) {
     __shared__ double blk[BLK][BLK + 1];
     __shared__ int s_item;
     const int lane = threadIdx.x;
+    const unsigned FULL = 0xffffffffu;
     for (;;) {
         if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
         __syncwarp();
@@ -156,44 +161,57 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
         double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
         for (int ch = 0; ch < nchunk; ++ch) {
             const int cx = ch * BLK;
-#pragma unroll 8
-            for (int rr = 0; rr < BLK; ++rr) blk[rr][lane] = rows[(size_t)rr * n + cx + lane];
+            const int il = cx + lane;
+            const double tds = il < m ? ds[il] : 0.0, tdl = il < m ? dl[il] : 0.0, trd = il < m ? rd[il] : 0.0;
+            double v[BLK];
+#pragma unroll
+            for (int rr = 0; rr < BLK; ++rr) v[rr] = rows[(size_t)rr * n + il];
+#pragma unroll
+            for (int rr = 0; rr < BLK; ++rr) blk[rr][lane] = v[rr];
             __syncwarp();
-#pragma unroll 4
+#pragma unroll
             for (int k = 0; k < BLK; ++k) {
                 const int i = cx + k;
-                const double v = blk[lane][k];
+                const double x = blk[lane][k];
+                const double a_s = __shfl_sync(FULL, tds, k), a_l = __shfl_sync(FULL, tdl, k);
+                const double a_r = __shfl_sync(FULL, trd, k);
                 if (i < m) {
-                    double t = fma(-ds[i], b2, v);
-                    t = fma(-dl[i], b1, t);
-                    t *= rd[i];
+                    double t = fma(-a_s, b2, x);
+                    t = fma(-a_l, b1, t);
+                    t *= a_r;
                     b2 = b1;
                     b1 = t;
                     blk[lane][k] = t;
                 } else if (i == m) {
-                    r2 = v;
+                    r2 = x;
                 } else {
-                    r1 = v;
+                    r1 = x;
                 }
             }
             __syncwarp();
-#pragma unroll 8
-            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + cx + lane] = blk[rr][lane];
+#pragma unroll
+            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + il] = blk[rr][lane];
             __syncwarp();
         }
         // backward substitution, chunks in reverse
         double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
         for (int ch = nchunk - 1; ch >= 0; --ch) {
             const int cx = ch * BLK;
-#pragma unroll 8
-            for (int rr = 0; rr < BLK; ++rr) blk[rr][lane] = rows[(size_t)rr * n + cx + lane];
+            const int il = cx + lane;
+            const double tdu = il < m ? du[il] : 0.0, tdw = il < m ? dw[il] : 0.0;
+            double v[BLK];
+#pragma unroll
+            for (int rr = 0; rr < BLK; ++rr) v[rr] = rows[(size_t)rr * n + il];
+#pragma unroll
+            for (int rr = 0; rr < BLK; ++rr) blk[rr][lane] = v[rr];
             __syncwarp();
-#pragma unroll 4
+#pragma unroll
             for (int k = BLK - 1; k >= 0; --k) {
                 const int i = cx + k;
+                const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
                 if (i < m) {
-                    double y = fma(-du[i], f1, blk[lane][k]);
-                    y = fma(-dw[i], f2, y);
+                    double y = fma(-a_u, f1, blk[lane][k]);
+                    y = fma(-a_w, f2, y);
                     f2 = f1;
                     f1 = y;
                     blk[lane][k] = y;
@@ -204,8 +222,8 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
                 }
             }
             __syncwarp();
-#pragma unroll 8
-            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + cx + lane] = blk[rr][lane];
+#pragma unroll
+            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + il] = blk[rr][lane];
             __syncwarp();
         }
         // the last two unknowns through the 2 x 2 Schur complement (BatchHyper.cu:195-227)
@@ -229,11 +247,15 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
 // ------------------------------------------------------------------------------------------------
 // K3: y sweep (lane = column) + the update
 // ------------------------------------------------------------------------------------------------
+// Rows are taken 32 at a time: the batch's field values are loaded into registers first (32 loads
+// in flight per lane) and the batch's table entries / row ends are loaded coalesced and broadcast
+// with shuffles, so the FP64 recurrence does not wait on memory.
 __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restrict__ grids,
                                                         const Item* __restrict__ items, int n_items, int parity,
                                                         unsigned int* counter) {
     __shared__ int s_item;
     const int lane = threadIdx.x;
+    const unsigned FULL = 0xffffffffu;
     for (;;) {
         if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
         __syncwarp();
@@ -253,39 +275,72 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
         const double* inv2 = tab + 6 * m;
         const int x = item.block * BLK + lane;
         double* t = gd.tmp;
-        // x sweep's rank-2 correction for this column (BatchHyper.cu:233-259): applied on read
-        const double cx1 = (x < m) ? inv1[x] : 0.0;
-        const double cx2 = (x < m) ? inv2[x] : 0.0;
         const double* ends = gd.ends;
+        // x sweep's rank-2 correction for this column (BatchHyper.cu:233-259): applied on read
         const bool corr = x < m;
-#define CH_XVAL(y) (corr ? fma(-cx1, ends[2 * (y)], fma(-cx2, ends[2 * (y) + 1], t[(size_t)(y) * n + x])) \
-                         : t[(size_t)(y) * n + x])
+        const double cx1 = corr ? inv1[x] : 0.0;
+        const double cx2 = corr ? inv2[x] : 0.0;
+        const int nb = n / BLK;
         // forward elimination along y
-        double b1 = 0.0, b2 = 0.0;
-#pragma unroll 4
-        for (int y = 0; y < m; ++y) {
-            double v = fma(-ds[y], b2, CH_XVAL(y));
-            v = fma(-dl[y], b1, v);
-            v *= rd[y];
-            b2 = b1;
-            b1 = v;
-            t[(size_t)y * n + x] = v;
+        double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
+        for (int bb = 0; bb < nb; ++bb) {
+            const int yb = bb * BLK, yl = yb + lane;
+            const double tds = yl < m ? ds[yl] : 0.0, tdl = yl < m ? dl[yl] : 0.0, trd = yl < m ? rd[yl] : 0.0;
+            const double e2 = ends[2 * yl], e1 = ends[2 * yl + 1];
+            double v[BLK];
+#pragma unroll
+            for (int k = 0; k < BLK; ++k) v[k] = t[(size_t)(yb + k) * n + x];
+#pragma unroll
+            for (int k = 0; k < BLK; ++k) {
+                const int y = yb + k;
+                const double c2 = __shfl_sync(FULL, e2, k), c1 = __shfl_sync(FULL, e1, k);
+                const double a_s = __shfl_sync(FULL, tds, k), a_l = __shfl_sync(FULL, tdl, k);
+                const double a_r = __shfl_sync(FULL, trd, k);
+                const double val = corr ? fma(-cx1, c2, fma(-cx2, c1, v[k])) : v[k];
+                if (y < m) {
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
+                    b2 = b1;
+                    b1 = w;
+                    v[k] = w;
+                } else if (y == m) {
+                    r2 = val;
+                } else {
+                    r1 = val;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < BLK; ++k)
+                if (yb + k < m) t[(size_t)(yb + k) * n + x] = v[k];
         }
-        const double r2 = CH_XVAL(m), r1 = CH_XVAL(m + 1);
-#undef CH_XVAL
         // backward substitution
         double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
-#pragma unroll 4
-        for (int y = m - 1; y >= 0; --y) {
-            double v = fma(-du[y], f1, t[(size_t)y * n + x]);
-            v = fma(-dw[y], f2, v);
-            f2 = f1;
-            f1 = v;
-            t[(size_t)y * n + x] = v;
-            if (y == m - 1) ym1 = v;
-            if (y == m - 2) ym2 = v;
-            if (y == 1) y1v = v;
-            if (y == 0) y0v = v;
+        for (int bb = nb - 1; bb >= 0; --bb) {
+            const int yb = bb * BLK, yl = yb + lane;
+            const double tdu = yl < m ? du[yl] : 0.0, tdw = yl < m ? dw[yl] : 0.0;
+            double v[BLK];
+#pragma unroll
+            for (int k = 0; k < BLK; ++k) v[k] = (yb + k < m) ? t[(size_t)(yb + k) * n + x] : 0.0;
+#pragma unroll
+            for (int k = BLK - 1; k >= 0; --k) {
+                const int y = yb + k;
+                const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
+                if (y < m) {
+                    double w = fma(-a_u, f1, v[k]);
+                    w = fma(-a_w, f2, w);
+                    f2 = f1;
+                    f1 = w;
+                    v[k] = w;
+                    if (y == m - 1) ym1 = w;
+                    if (y == m - 2) ym2 = w;
+                    if (y == 1) y1v = w;
+                    if (y == 0) y0v = w;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < BLK; ++k)
+                if (yb + k < m) t[(size_t)(yb + k) * n + x] = v[k];
         }
         const double* om = tab + 7 * m;
         const double a = om[4], b = om[5], d = om[6], e = om[7];
@@ -296,14 +351,27 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
         // cNew = cBar + delta over cOld (cuPentCahnADI.cu:58-69, 89-100)
         const double* cur = parity ? gd.buf[1] : gd.buf[0];
         double* old = parity ? gd.buf[0] : gd.buf[1];
-#pragma unroll 4
-        for (int y = 0; y < n; ++y) {
-            const size_t k = (size_t)y * n + x;
-            double dlt;
-            if (y < m) dlt = fma(-inv1[y], x2, fma(-inv2[y], x1, t[k]));
-            else dlt = (y == m) ? x2 : x1;
-            const double cbar = fma(2.0, cur[k], -old[k]);
-            old[k] = cbar + dlt;
+        for (int bb = 0; bb < nb; ++bb) {
+            const int yb = bb * BLK, yl = yb + lane;
+            const double ti1 = yl < m ? inv1[yl] : 0.0, ti2 = yl < m ? inv2[yl] : 0.0;
+            double v[BLK], cv[BLK], ov[BLK];
+#pragma unroll
+            for (int k = 0; k < BLK; ++k) {
+                const size_t q = (size_t)(yb + k) * n + x;
+                v[k] = (yb + k < m) ? t[q] : 0.0;
+                cv[k] = cur[q];
+                ov[k] = old[q];
+            }
+#pragma unroll
+            for (int k = 0; k < BLK; ++k) {
+                const int y = yb + k;
+                const double a1 = __shfl_sync(FULL, ti1, k), a2 = __shfl_sync(FULL, ti2, k);
+                double dlt;
+                if (y < m) dlt = fma(-a1, x2, fma(-a2, x1, v[k]));
+                else dlt = (y == m) ? x2 : x1;
+                const double cbar = fma(2.0, cv[k], -ov[k]);
+                old[(size_t)y * n + x] = cbar + dlt;
+            }
         }
     }
 }
