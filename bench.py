@@ -332,10 +332,12 @@ def run_gpu(args, world, rank, local):
         del inp32, outs32, hs32, keep32
         torch.cuda.synchronize(dev)
 
-    # ---- e2e: reference-facing API with host buffers (managed memory, numTiles=4, HOST offload) ----
-    e2e = None
+    # ---- e2e: reference-facing API with host buffers (numTiles=4, HOST offload) ----
+    e2e = e2e_managed = None
     if not args.skip_e2e:
-        e2e = run_e2e(args, cs, np, local, ops)
+        e2e = run_e2e(args, cs, np, local, ops, "pinned")
+        if not args.skip_e2e_managed:
+            e2e_managed = run_e2e(args, cs, np, local, ops, "managed", steps=1)
 
     # ---- CPU baseline (rank 0 only) ----
     cpu = None
@@ -386,6 +388,8 @@ def run_gpu(args, world, rank, local):
             line["fp32"] = fp32
         if e2e is not None:
             line["e2e"] = e2e
+        if e2e_managed is not None:
+            line["e2e_managed"] = e2e_managed
         if cpu is not None:
             line["cpu_baseline"] = cpu
         if ch_batched is not None:
@@ -398,53 +402,69 @@ def run_gpu(args, world, rank, local):
         pg.destroy_process_group()
 
 
-def run_e2e(args, cs, np, local, ops):
-    """Same sweep through the reference-facing API on host (managed) buffers: numTiles=4, HOST offload.
-    Each Compute streams its tiles to the GPU and back (cudaMemPrefetchAsync), inside the timed region."""
+def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
+    """The same sweep through the reference-facing API on host buffers, numTiles=4, HOST offload,
+    host<->device traffic inside the timed region.
+
+    kind "pinned": fields in pinned host memory; each Compute streams the rows through device staging
+    slots (copy-in, kernel and copy-out of successive chunks overlap). kind "managed": fields in managed
+    memory, the reference's own HOST path (cudaMemPrefetchAsync of each tile to the device and back).
+    The byte counts are the library's own counters of what Compute moved."""
     import ctypes
 
     n = args.e2e_n
+    steps = steps or args.e2e_steps
     nbytes = n * n * 8
     lib = cs.lib()
+    allocs = []
 
-    def managed(nb):
+    def host(nb):
         p = ctypes.c_void_p()
-        cs._check(lib.custen_malloc_managed(ctypes.byref(p), nb))
+        fn = lib.custen_malloc_host if kind == "pinned" else lib.custen_malloc_managed
+        cs._check(fn(ctypes.byref(p), nb))
+        allocs.append(p.value)
         return p.value
 
+    def arr(ptr, count):
+        return np.frombuffer((ctypes.c_char * (8 * count)).from_address(ptr), dtype=np.float64)
+
     from tests.helpers import field
-    inp = managed(nbytes)
-    arr = np.frombuffer((ctypes.c_char * nbytes).from_address(inp), dtype=np.float64).reshape(n, n)
-    arr[:] = field(n, n, 1)
-    outs, hs, ws = [], [], []
+    inp = host(nbytes)
+    arr(inp, n * n)[:] = field(n, n, 1).ravel()
+    outs, hs = [], []
     for (nm, v, H, L, R, V, T, B, w, fun, _) in ops:
-        o = managed(nbytes)
-        np.frombuffer((ctypes.c_char * nbytes).from_address(o), dtype=np.float64)[:] = 0.0
-        wp = managed(8 * len(w))
-        np.frombuffer((ctypes.c_char * (8 * len(w))).from_address(wp), dtype=np.float64)[:] = w
+        o = host(nbytes)
+        arr(o, n * n)[:] = 0.0
+        wp = host(8 * len(w))
+        arr(wp, len(w))[:] = w
         func = cs.builtin_function(fun, cs.F64) if fun >= 0 else None
         hs.append(cs.Stencil(v, n, n, o, inp, wp, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=4, block_x=32, block_y=8,
                              ncoef=len(w), func=func, device=local))
         outs.append(o)
-        ws.append(wp)
     for h in hs:
         h.compute(cs.HOST)
     cs._check(lib.custen_device_synchronize())
+    h2d0, d2h0 = cs.transfer_bytes()
+    launches0 = cs.kernel_launches()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(steps):
         for h in hs:
             h.compute(cs.HOST)
         cs._check(lib.custen_device_synchronize())
-        _ = float(np.frombuffer((ctypes.c_char * 8).from_address(outs[-1]), dtype=np.float64)[0])  # host read
-    dt = (time.perf_counter() - t0) / args.e2e_steps
+        _ = float(arr(outs[-1], 1)[0])  # host read of the result
+    dt = (time.perf_counter() - t0) / steps
+    h2d1, d2h1 = cs.transfer_bytes()
+    launches = (cs.kernel_launches() - launches0) // steps
     for h in hs:
         h.destroy()
-    for p in outs + ws + [inp]:
-        lib.custen_free(p)
-    per_compute = 2 * nbytes   # input and output tiles to the device, then both back
+    for p in allocs:
+        (lib.custen_free_host if kind == "pinned" else lib.custen_free)(p)
+    what = ("pinned host buffers, rows streamed through device staging slots in 32 MiB chunks"
+            if kind == "pinned" else "managed buffers, tiles prefetched to the device and back (reference HOST path)")
     return {"value": round(len(ops) * n * n / dt / 1e9, 3), "unit": "Gpts/s",
-            "h2d_bytes_per_step": per_compute * len(ops), "d2h_bytes_per_step": per_compute * len(ops),
-            "path": f"managed host buffers {n}^2, numTiles=4, Compute(HOST) per operator (tile streaming)"}
+            "h2d_bytes_per_step": (h2d1 - h2d0) // steps, "d2h_bytes_per_step": (d2h1 - d2h0) // steps,
+            "ms_per_step": round(dt * 1e3, 2), "steps": steps, "kernel_launches_per_step": launches,
+            "path": f"{n}^2, 12 operators, numTiles=4, Compute(HOST) per operator; {what}"}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -555,10 +575,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--e2e-n", type=int, default=16384)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-rows", type=int, default=4096)
     ap.add_argument("--skip-fp32", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-e2e-managed", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-ch", action="store_true")
     ap.add_argument("--skip-served", action="store_true")

@@ -50,6 +50,10 @@ def lib() -> ctypes.CDLL:
         L.custen_last_error.restype = ctypes.c_char_p
         L.custen_kernel_launches.restype = ull
         L.custen_kernel_launches_tma.restype = ull
+        L.custen_transfer_bytes.argtypes = [ctypes.POINTER(ull), ctypes.POINTER(ull)]
+        L.custen_transfer_bytes.restype = None
+        L.custen_set_stage_chunk_bytes.argtypes = [sz]
+        L.custen_set_stage_chunk_bytes.restype = None
         L.custen_device_error.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
         L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
         L.custen_compute.argtypes = [vp, i]
@@ -133,6 +137,18 @@ def kernel_launches() -> int:
 
 def kernel_launches_tma() -> int:
     return int(lib().custen_kernel_launches_tma())
+
+
+def transfer_bytes() -> tuple:
+    """(host->device, device->host) bytes moved by Compute since the library was loaded."""
+    h2d, d2h = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    lib().custen_transfer_bytes(ctypes.byref(h2d), ctypes.byref(d2h))
+    return int(h2d.value), int(d2h.value)
+
+
+def set_stage_chunk_bytes(nbytes: int) -> None:
+    """Chunk size for streaming host-resident fields through the GPU (0: default 32 MiB)."""
+    lib().custen_set_stage_chunk_bytes(int(nbytes))
 
 
 def device_error(clear: bool = True) -> int:

@@ -117,7 +117,17 @@ struct PlanPrivate {
     cudaStream_t user_stream;
     int use_user_stream;
     unsigned long long launches;   // kernels launched by this handle (for instrumentation)
+    // Host-resident fields (pinned or system memory) are streamed through device staging slots:
+    // kStageSlots slots of (T + chunk + B) input rows and chunk output rows, plus the weights.
+    // Allocated at the first such Compute, freed by Destroy.
+    void* stage;
+    size_t stage_slot_bytes;
+    int stage_rows;               // rows per chunk
+    int stage_events_ready;
+    cudaEvent_t stage_ev[3 * 3];  // per slot: inputs copied in, kernel done, outputs copied out
 };
+
+constexpr int kStageSlots = 3;
 
 struct StreamBlock {
     cudaStream_t streams[3];

@@ -9,6 +9,7 @@
 // per tile reads its halo rows through the handle's boundaryTop/boundaryBottom pointers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -33,6 +34,9 @@ __device__ unsigned int g_custen_device_error = 0;
 static thread_local std::string g_last_error;
 static std::atomic<unsigned long long> g_launches{0};
 static std::atomic<unsigned long long> g_launches_tma{0};
+static std::atomic<unsigned long long> g_h2d_bytes{0};   // host -> device bytes moved by Compute
+static std::atomic<unsigned long long> g_d2h_bytes{0};   // device -> host bytes moved by Compute
+static std::atomic<size_t> g_stage_chunk_bytes{(size_t)32 << 20};   // staging chunk size, host-resident fields
 
 enum { ST_OK = 0, ST_CUDA = 1, ST_ARG = 2, ST_UNSUPPORTED = 3 };
 
@@ -159,6 +163,10 @@ int create_plan(cuSten_t* h, int variant, int dtype, int dev, int numTiles, int 
     p.user_stream = nullptr;
     p.use_user_stream = 0;
     p.launches = 0;
+    p.stage = nullptr;
+    p.stage_slot_bytes = 0;
+    p.stage_rows = 0;
+    p.stage_events_ready = 0;
 
     const int esz = dtype == DT_F64 ? 8 : 4;
     const int dir = variant_dir(variant);
@@ -223,6 +231,12 @@ static int destroy_plan(cuSten_t* h) {
     for (int ev = 0; ev < 2; ++ev) {
         cudaError_t e = cudaEventDestroy(h->events[ev]);
         if (e != cudaSuccess && st == ST_OK) st = fail_cuda(e, "Destroying event");
+    }
+    if (blk->priv.stage_events_ready)
+        for (int ev = 0; ev < 3 * kStageSlots; ++ev) cudaEventDestroy(blk->priv.stage_ev[ev]);
+    if (blk->priv.stage) {
+        cudaError_t e = cudaFree(blk->priv.stage);
+        if (e != cudaSuccess && st == ST_OK) st = fail_cuda(e, "Freeing staging buffers");
     }
     blk->priv.magic = 0;
     free(blk);
@@ -295,6 +309,165 @@ static cudaError_t launch(const StencilArgs& a, int dtype, cudaStream_t s, PlanP
     return e;
 }
 
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Copies rows [r_begin, r_end) of tile t's input, in tile-local numbering, to dst. Rows below 0
+// come from the tile's top halo rows, rows at or past nyTile from its bottom halo rows (the
+// handle's boundaryTop/boundaryBottom pointers, as the reference's per-tile kernels read them).
+static cudaError_t copy_tile_rows(const cuSten_t* h, int t, int r_begin, int r_end, char* dst, size_t row_bytes,
+                                  int T, cudaStream_t s, unsigned long long* moved) {
+    const int nyT = h->nyTile;
+    while (r_begin < r_end) {
+        const char* src;
+        int seg_end;
+        if (r_begin < 0) {
+            src = reinterpret_cast<const char*>(h->boundaryTop[t]) + (size_t)(T + r_begin) * row_bytes;
+            seg_end = r_end < 0 ? r_end : 0;
+        } else if (r_begin < nyT) {
+            src = reinterpret_cast<const char*>(h->dataInput[t]) + (size_t)r_begin * row_bytes;
+            seg_end = r_end < nyT ? r_end : nyT;
+        } else {
+            src = reinterpret_cast<const char*>(h->boundaryBottom[t]) + (size_t)(r_begin - nyT) * row_bytes;
+            seg_end = r_end;
+        }
+        const size_t bytes = (size_t)(seg_end - r_begin) * row_bytes;
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s);
+        if (e != cudaSuccess) return e;
+        *moved += bytes;
+        dst += bytes;
+        r_begin = seg_end;
+    }
+    return cudaSuccess;
+}
+
+// Host-resident fields: the rows of every tile stream through device staging slots in chunks.
+// Chunk c copies its input rows and halo rows in on s_in, computes on s_comp and copies its output
+// rows back on s_out; kStageSlots chunks are in flight, so the two copy directions and the
+// kernels overlap. For the non-periodic variants the cells a Compute leaves untouched (the field's
+// first L and last max(L, R) columns, its first T and last B rows) are copied in first, so that the
+// whole chunk can be copied back unchanged.
+static int compute_staged(cuSten_t* h, PlanPrivate* p, StencilArgs& a, cudaStream_t s_comp, cudaStream_t s_in,
+                          cudaStream_t s_out) {
+    const int esz = p->dtype == DT_F64 ? 8 : 4;
+    const int nt = h->numTiles, nx = h->nx, ny = h->ny, nyT = h->nyTile;
+    const int dir = variant_dir(p->variant);
+    const bool periodic = variant_is_periodic(p->variant);
+    const int T = p->T, B = p->B;
+    const size_t row_bytes = (size_t)nx * esz;
+    if (!p->stage) {
+        // Chunks of about 32 MiB (custen_set_stage_chunk_bytes), a multiple of 32 rows where the tile
+        // allows (the TMA kernel's tile height), and never shorter than a halo.
+        const size_t target = g_stage_chunk_bytes.load();
+        int rows = (int)std::max<size_t>(1, target / row_bytes);
+        if (rows >= 32) rows -= rows % 32;
+        rows = std::max(rows, std::max(T, B));
+        rows = std::min(rows, nyT);
+        const size_t in_bytes = align256((size_t)(T + rows + B) * row_bytes);
+        const size_t out_bytes = align256((size_t)rows * row_bytes);
+        const size_t slot = in_bytes + out_bytes;
+        const size_t coef_bytes = align256((size_t)std::max(p->ncoef, 1) * esz);
+        CU_TRY(cudaMalloc(&p->stage, kStageSlots * slot + coef_bytes), "Allocating staging buffers");
+        p->stage_slot_bytes = slot;
+        p->stage_rows = rows;
+    }
+    if (!p->stage_events_ready) {
+        for (int ev = 0; ev < 3 * kStageSlots; ++ev)
+            CU_TRY(cudaEventCreateWithFlags(&p->stage_ev[ev], cudaEventDisableTiming), "Creating event");
+        p->stage_events_ready = 1;
+    }
+    const int rows = p->stage_rows;
+    const size_t slot_bytes = p->stage_slot_bytes;
+    const size_t in_bytes = align256((size_t)(T + rows + B) * row_bytes);
+    char* stage = static_cast<char*>(p->stage);
+    char* coef_dev = stage + kStageSlots * slot_bytes;
+    unsigned long long h2d = 0, d2h = 0;
+
+    // Weights (or Fun coefficients) once per Compute: the kernels then read device memory only.
+    // The copy waits for every kernel of the previous Compute that may still read the old ones.
+    for (int k = 0; k < kStageSlots; ++k) CU_TRY(cudaStreamWaitEvent(s_in, p->stage_ev[3 * k + 1], 0), "Ordering");
+    if (p->ncoef > 0) {
+        CU_TRY(cudaMemcpyAsync(coef_dev, a.coef, (size_t)p->ncoef * esz, cudaMemcpyDefault, s_in), "Copying weights");
+        h2d += (size_t)p->ncoef * esz;
+        a.coef = coef_dev;
+    }
+    const int wl = std::max(p->L, p->R);
+    int c = 0;
+    for (int t = 0; t < nt; ++t) {
+        for (int r0 = 0; r0 < nyT; r0 += rows, ++c) {
+            const int rc = std::min(rows, nyT - r0);
+            const int k = c % kStageSlots;
+            cudaEvent_t ev_in = p->stage_ev[3 * k], ev_kern = p->stage_ev[3 * k + 1], ev_out = p->stage_ev[3 * k + 2];
+            char* in_slot = stage + (size_t)k * slot_bytes;
+            char* out_slot = in_slot + in_bytes;
+            const int gy0 = t * nyT + r0;
+            const bool has_top = dir != 0 && T > 0 && (periodic || gy0 > 0);
+            const bool has_bot = dir != 0 && B > 0 && (periodic || gy0 + rc < ny);
+            // the slot is free once its previous kernel and its previous copy-out are done
+            CU_TRY(cudaStreamWaitEvent(s_in, ev_kern, 0), "Ordering copy after kernel");
+            CU_TRY(cudaStreamWaitEvent(s_in, ev_out, 0), "Ordering copy after copy-out");
+            char* body = in_slot + (size_t)T * row_bytes;
+            CU_TRY(copy_tile_rows(h, t, has_top ? r0 - T : r0, r0 + rc + (has_bot ? B : 0),
+                                  has_top ? in_slot : body, row_bytes, T, s_in, &h2d),
+                   "Copying input rows to the device");
+            if (!periodic) {
+                char* host_out = reinterpret_cast<char*>(h->dataOutput[t]) + (size_t)r0 * row_bytes;
+                if (dir != 0) {
+                    // field rows [0, T) and [ny - B, ny) that fall in this chunk
+                    const int lo[2] = {0, ny - B}, hi[2] = {T, ny};
+                    for (int q = 0; q < 2; ++q) {
+                        const int a0 = std::max(lo[q], gy0), a1 = std::min(hi[q], gy0 + rc);
+                        if (a1 <= a0) continue;
+                        const size_t off = (size_t)(a0 - gy0) * row_bytes, bytes = (size_t)(a1 - a0) * row_bytes;
+                        CU_TRY(cudaMemcpyAsync(out_slot + off, host_out + off, bytes, cudaMemcpyDefault, s_in),
+                               "Copying untouched output rows");
+                        h2d += bytes;
+                    }
+                }
+                if (dir != 1) {
+                    if (p->L > 0) {
+                        CU_TRY(cudaMemcpy2DAsync(out_slot, row_bytes, host_out, row_bytes, (size_t)p->L * esz, rc,
+                                                 cudaMemcpyDefault, s_in),
+                               "Copying untouched output columns");
+                        h2d += (size_t)p->L * esz * rc;
+                    }
+                    if (wl > 0) {
+                        const size_t off = (size_t)(nx - wl) * esz;
+                        CU_TRY(cudaMemcpy2DAsync(out_slot + off, row_bytes, host_out + off, row_bytes, (size_t)wl * esz,
+                                                 rc, cudaMemcpyDefault, s_in),
+                               "Copying untouched output columns");
+                        h2d += (size_t)wl * esz * rc;
+                    }
+                }
+            }
+            CU_TRY(cudaEventRecord(ev_in, s_in), "Recording event");
+            CU_TRY(cudaStreamWaitEvent(s_comp, ev_in, 0), "Ordering kernel after copy-in");
+            a.in = body;
+            a.out = out_slot;
+            a.rows = rc;
+            a.row0 = gy0;
+            a.top = in_slot;
+            a.bot = body + (size_t)rc * row_bytes;
+            a.has_top = has_top;
+            a.has_bot = has_bot;
+            a.vec_ok = row_bytes % 16 == 0;
+            CU_TRY(launch(a, p->dtype, s_comp, p), "Computing stencil chunk");
+            CU_TRY(cudaEventRecord(ev_kern, s_comp), "Recording event");
+            CU_TRY(cudaStreamWaitEvent(s_out, ev_kern, 0), "Ordering copy-out after kernel");
+            char* host_out = reinterpret_cast<char*>(h->dataOutput[t]) + (size_t)r0 * row_bytes;
+            CU_TRY(cudaMemcpyAsync(host_out, out_slot, (size_t)rc * row_bytes, cudaMemcpyDefault, s_out),
+                   "Copying output rows to the host");
+            d2h += (size_t)rc * row_bytes;
+            CU_TRY(cudaEventRecord(ev_out, s_out), "Recording event");
+        }
+    }
+    // Work issued later on the compute stream follows the last copy-out.
+    for (int k = 0; k < kStageSlots; ++k)
+        CU_TRY(cudaStreamWaitEvent(s_comp, p->stage_ev[3 * k + 2], 0), "Ordering compute after copies");
+    g_h2d_bytes.fetch_add(h2d, std::memory_order_relaxed);
+    g_d2h_bytes.fetch_add(d2h, std::memory_order_relaxed);
+    return ST_OK;
+}
+
 int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
     PlanPrivate* p = priv_of(h);
     if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
@@ -339,6 +512,7 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
     }
 
     const int kind = memory_kind(in0);
+    const int kind_out = memory_kind(out0);
     p->mem_kind = kind;
     const bool row_aligned = ((size_t)nx * esz) % 16 == 0;
 
@@ -356,8 +530,14 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
                    (!a.has_bot || aligned16(a.bot));
     };
 
+    if (kind == 2 || kind_out == 2) {
+        // Pinned or system memory: stream the rows through device staging slots.
+        cudaStream_t s_out = explicit_stream ? *explicit_stream
+                                             : (p->use_user_stream ? p->user_stream : h->streams[2]);
+        return compute_staged(h, p, a, s, copy_s, s_out);
+    }
     if (kind != 1) {
-        // Device-resident (or directly addressable) data: no migration needed.
+        // Device-resident data: no copies.
         if (contiguous) {
             fill_launch(0, nt);
             CU_TRY(launch(a, p->dtype, s, p), "Computing stencil");
@@ -377,7 +557,9 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
     const int dev = h->deviceNum;
     const size_t halo_top_bytes = (size_t)p->T * nx * esz, halo_bot_bytes = (size_t)p->B * nx * esz;
     CU_TRY(prefetch(a.coef, (size_t)p->ncoef * esz, dev, copy_s), "Prefetching weights");
+    unsigned long long moved_in = 0, moved_out = 0;
     auto prefetch_tile = [&](int t) -> cudaError_t {
+        moved_in += 2 * tile_bytes + (dir != 0 ? halo_top_bytes + halo_bot_bytes : 0);
         cudaError_t e = prefetch(h->dataInput[t], tile_bytes, dev, copy_s);
         if (e == cudaSuccess) e = prefetch(h->dataOutput[t], tile_bytes, dev, copy_s);
         if (e == cudaSuccess && dir != 0 && halo_top_bytes) e = prefetch(h->boundaryTop[t], halo_top_bytes, dev, copy_s);
@@ -391,6 +573,7 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
         fill_launch(t, 1);
         CU_TRY(launch(a, p->dtype, s, p), "Computing stencil tile");
         if (offload == HOST) {
+            moved_out += 2 * tile_bytes;
             CU_TRY(prefetch(h->dataOutput[t], tile_bytes, -1, s), "Offloading output tile");
             CU_TRY(prefetch(h->dataInput[t], tile_bytes, -1, s), "Offloading input tile");
         }
@@ -401,6 +584,8 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
         CU_TRY(cudaEventRecord(h->events[0], copy_s), "Recording event");
         CU_TRY(cudaStreamWaitEvent(s, h->events[0], 0), "Ordering compute after copies");
     }
+    g_h2d_bytes.fetch_add(moved_in, std::memory_order_relaxed);
+    g_d2h_bytes.fetch_add(moved_out, std::memory_order_relaxed);
     return ST_OK;
 }
 
@@ -524,6 +709,11 @@ int custen_sizeof_handle(void) { return (int)sizeof(cuSten_t); }
 const char* custen_last_error(void) { return g_last_error.c_str(); }
 unsigned long long custen_kernel_launches(void) { return g_launches.load(); }
 unsigned long long custen_kernel_launches_tma(void) { return g_launches_tma.load(); }
+void custen_set_stage_chunk_bytes(size_t bytes) { g_stage_chunk_bytes.store(bytes ? bytes : (size_t)32 << 20); }
+void custen_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h) {
+    if (h2d) *h2d = g_h2d_bytes.load();
+    if (d2h) *d2h = g_d2h_bytes.load();
+}
 
 int custen_create(cuSten_t* h, int variant, int dtype, int dev, int nt, int nx, int ny, int bx, int by, void* out,
                   void* in, void* coef, int H, int L, int R, int V, int T, int B, int ncoef, void* func) {

@@ -37,6 +37,12 @@ int custen_sizeof_handle(void);               /* sizeof(cuSten_t): 200 on LP64 *
 const char* custen_last_error(void);
 unsigned long long custen_kernel_launches(void);   /* kernels launched by this library so far */
 unsigned long long custen_kernel_launches_tma(void);   /* of which used the TMA-staged stencil kernel */
+/* Bytes Compute has moved host -> device and device -> host since the library was loaded (managed
+ * prefetches and the staged copies of pinned / system-memory fields). No reference counterpart. */
+void custen_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h);
+/* Fields in pinned or system memory are streamed through device staging slots in chunks of about
+ * `bytes` (0: the default, 32 MiB); applies to handles whose first such Compute comes later. */
+void custen_set_stage_chunk_bytes(size_t bytes);
 
 /* ---- handle life cycle: generic form ----
  * H/L/R: window width and extents in x; V/T/B in y. X variants: V=1, T=B=0; Y variants: H=1, L=R=0.

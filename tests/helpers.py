@@ -54,6 +54,39 @@ class DeviceBuffer:
             pass
 
 
+class HostBuffer:
+    """Pinned host allocation made through the C-ABI, with a numpy view."""
+
+    def __init__(self, nbytes: int):
+        self.nbytes = nbytes
+        p = ctypes.c_void_p()
+        cs._check(cs.lib().custen_malloc_host(ctypes.byref(p), max(nbytes, 16)))
+        self.ptr = int(p.value)
+
+    @classmethod
+    def from_array(cls, a: np.ndarray) -> "HostBuffer":
+        b = cls(a.nbytes)
+        b.view(a.shape, a.dtype)[...] = a
+        return b
+
+    def view(self, shape, dtype) -> np.ndarray:
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        assert n <= self.nbytes
+        buf = (ctypes.c_char * n).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self) -> None:
+        if self.ptr:
+            cs.lib().custen_free_host(self.ptr)
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 def field(nx: int, ny: int, seed: int, dtype=np.float64) -> np.ndarray:
     """sin(3x)cos(5y) + U(-1e-3, 1e-3) on [0,2pi)^2 (the benchmark field)."""
     rng = np.random.default_rng(seed)

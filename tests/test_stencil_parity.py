@@ -9,7 +9,7 @@ import pytest
 
 import custen_gb300 as cs
 import oracle
-from tests.helpers import DeviceBuffer, field, sentinel, weights_for
+from tests.helpers import DeviceBuffer, HostBuffer, field, sentinel, weights_for
 
 pytestmark = pytest.mark.gpu
 
@@ -28,7 +28,9 @@ def geometry(variant, kind):
 
 
 def run_both(variant, nx, ny, tiles, bx, by, geom, dtype=np.float64, fun_id=-1, seed=0, managed=False,
-             offload=cs.DEVICE):
+             offload=cs.DEVICE, mem=None):
+    """mem: "device" (default), "managed", "pinned" (cudaMallocHost) or "pageable" (numpy memory)."""
+    mem = mem or ("managed" if managed else "device")
     H, L, R, V, T, B = geom
     inp = field(nx, ny, seed, dtype)
     fun = fun_id >= 0
@@ -44,15 +46,28 @@ def run_both(variant, nx, ny, tiles, bx, by, geom, dtype=np.float64, fun_id=-1, 
                         B=B, fun_id=fun_id)
 
     dt = cs.F64 if dtype == np.float64 else cs.F32
-    d_in = DeviceBuffer.from_array(inp, managed)
-    d_out = DeviceBuffer.from_array(pre, managed)
-    d_c = DeviceBuffer.from_array(coef, managed)
+    if mem in ("device", "managed"):
+        d_in = DeviceBuffer.from_array(inp, mem == "managed")
+        d_out = DeviceBuffer.from_array(pre, mem == "managed")
+        d_c = DeviceBuffer.from_array(coef, mem == "managed")
+        ptrs = (d_out.ptr, d_in.ptr, d_c.ptr)
+    elif mem == "pinned":
+        d_in, d_out, d_c = HostBuffer.from_array(inp), HostBuffer.from_array(pre), HostBuffer.from_array(coef)
+        ptrs = (d_out.ptr, d_in.ptr, d_c.ptr)
+    else:
+        d_in, d_out, d_c = inp.copy(), pre.copy(), coef.copy()
+        ptrs = (d_out.ctypes.data, d_in.ctypes.data, d_c.ctypes.data)
     func = cs.builtin_function(fun_id, dt) if fun else None
-    s = cs.Stencil(variant, nx, ny, d_out.ptr, d_in.ptr, d_c.ptr, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=tiles,
+    s = cs.Stencil(variant, nx, ny, ptrs[0], ptrs[1], ptrs[2], H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=tiles,
                    block_x=bx, block_y=by, dtype=dt, ncoef=ncoef, func=func)
     s.compute(offload)
     cs._check(cs.lib().custen_device_synchronize())
-    got = d_out.view((ny, nx), dtype).copy() if managed else d_out.download((ny, nx), dtype)
+    if mem == "device":
+        got = d_out.download((ny, nx), dtype)
+    elif mem == "pageable":
+        got = d_out.copy()
+    else:
+        got = d_out.view((ny, nx), dtype).copy()
     s.destroy()
     return got, ref, st, pre
 
@@ -125,6 +140,48 @@ def test_managed_memory_tile_streaming(gpu, variant):
     fun_id = FUN_IDS[d][1] if variant == cs.XYNPFUN else -1
     got, ref, st, pre = run_both(variant, 64, 128, 4, 16, 8, geometry(variant, "sym"), fun_id=fun_id, seed=5,
                                  managed=True, offload=cs.HOST)
+    check(got, ref, st, pre)
+
+
+@pytest.fixture
+def small_chunks():
+    """Host-resident fields stream in chunks of a few rows, so a tile spans several chunks and the
+    staging slots are reused within one Compute."""
+    cs.set_stage_chunk_bytes(4096)
+    yield
+    cs.set_stage_chunk_bytes(0)
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=cs.VARIANT_NAMES)
+@pytest.mark.parametrize("tiles", [1, 4])
+@pytest.mark.parametrize("mem", ["pinned", "pageable"])
+def test_host_memory_streaming(gpu, small_chunks, variant, tiles, mem):
+    """Fields in pinned or pageable host memory, HOST offload: rows stream through the device staging
+    slots (several chunks per tile, halos across chunk and tile borders) and every written point is
+    bit-identical to the oracle; the untouched border keeps its values."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    fun = variant in (cs.XPFUN, cs.XNPFUN, cs.YPFUN, cs.YNPFUN, cs.XYPFUN, cs.XYNPFUN)
+    geom = geometry(variant, "asym")
+    fun_id = -1
+    if fun:
+        fun_id = FUN_IDS[d][1]
+        geom = {0: (5, 2, 2, 1, 0, 0), 1: (1, 0, 0, 5, 2, 2), 2: (5, 2, 2, 5, 2, 2)}[d]
+    h2d0, d2h0 = cs.transfer_bytes()
+    nx, ny = 64, 256
+    got, ref, st, pre = run_both(variant, nx, ny, tiles, 16, 8, geom, fun_id=fun_id, seed=31 + variant, mem=mem,
+                                 offload=cs.HOST)
+    check(got, ref, st, pre)
+    h2d1, d2h1 = cs.transfer_bytes()
+    assert d2h1 - d2h0 == nx * ny * 8            # every output row comes back once
+    assert h2d1 - h2d0 >= nx * ny * 8            # every input row goes in at least once
+
+
+@pytest.mark.parametrize("variant", [cs.XP, cs.YNP, cs.XYP, cs.XYNP])
+def test_host_memory_default_chunks_f32(gpu, variant):
+    """Pinned FP32 fields at the default chunk size, DEVICE offload (the output still lands in host
+    memory: it is where the field lives)."""
+    got, ref, st, pre = run_both(variant, 128, 128, 2, 32, 8, geometry(variant, "sym"), dtype=np.float32, seed=8,
+                                 mem="pinned")
     check(got, ref, st, pre)
 
 
