@@ -23,6 +23,7 @@ LIB_PATH = _PKG / "libcusten_gb300.so"
 XP, XNP, XPFUN, XNPFUN, YP, YNP, YPFUN, YNPFUN, XYP, XYNP, XYPFUN, XYNPFUN = range(12)
 VARIANT_NAMES = ["Xp", "Xnp", "XpFun", "XnpFun", "Yp", "Ynp", "YpFun", "YnpFun", "XYp", "XYnp", "XYpFun",
                  "XYnpFun"]
+XYWENOADVP = 12   # WENO5 advection, periodic (WenoAdvection)
 F64, F32 = 0, 1
 DEVICE, HOST = 0, 1
 HANDLE_BYTES = 200
@@ -56,6 +57,8 @@ def lib() -> ctypes.CDLL:
         L.custen_set_stage_chunk_bytes.restype = None
         L.custen_device_error.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
         L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
+        L.custen_create_2d_xyweno_adv_p.argtypes = [vp, i, i, i, i, i, i, ctypes.c_double, ctypes.c_double, vp, vp,
+                                                    vp, vp]
         L.custen_compute.argtypes = [vp, i]
         L.custen_compute_on_stream.argtypes = [vp, i, vp]
         L.custen_swap.argtypes = [vp, vp]
@@ -205,6 +208,21 @@ class Stencil:
             self.destroy()
         except Exception:
             pass
+
+
+class WenoAdvection(Stencil):
+    """cuStenCreate2DXYWENOADVp / Compute / Swap / Destroy: out = u * WENO5_x(in) + v * WENO5_y(in) on a
+    periodic grid with spacings dx, dy (cuSten_struct_functions.h:290-347)."""
+
+    def __init__(self, nx: int, ny: int, out, inp, u, v, *, dx: float, dy: float, num_tiles=1, block_x=32,
+                 block_y=8, device=0):
+        self.variant, self.dtype = XYWENOADVP, F64
+        self.nx, self.ny = nx, ny
+        self.handle = ctypes.create_string_buffer(HANDLE_BYTES)
+        self._alive = False
+        _check(lib().custen_create_2d_xyweno_adv_p(self.handle, device, num_tiles, nx, ny, block_x, block_y,
+                                                   float(dx), float(dy), addr(u), addr(v), addr(out), addr(inp)))
+        self._alive = True
 
 
 class CuStenT(ctypes.Structure):

@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPI
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
 # Translation units of the static drop-in library (the reference's libcuSten.a surface).
-LIB_SOURCES = ["plan.cu", "stencil_f64.cu", "stencil_f32.cu"]
+LIB_SOURCES = ["plan.cu", "stencil_f64.cu", "stencil_f32.cu", "weno.cu"]
 # Extra translation units of the shared library.
 SO_SOURCES = ["builtin_funs.cu", "probe.cu", "ch_solver.cu", "ch_server.cu"]
 

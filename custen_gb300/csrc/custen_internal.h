@@ -14,7 +14,8 @@ enum Variant : int {
     V_XP = 0, V_XNP = 1, V_XPFUN = 2, V_XNPFUN = 3,
     V_YP = 4, V_YNP = 5, V_YPFUN = 6, V_YNPFUN = 7,
     V_XYP = 8, V_XYNP = 9, V_XYPFUN = 10, V_XYNPFUN = 11,
-    V_COUNT = 12
+    V_COUNT = 12,          // the weighted / Fun variants above
+    V_XYWENOADVP = 12      // WENO5 advection, periodic (its own Create argument list)
 };
 
 enum DType : int { DT_F64 = 0, DT_F32 = 1 };
@@ -22,7 +23,7 @@ enum DType : int { DT_F64 = 0, DT_F32 = 1 };
 __host__ __device__ inline bool variant_is_fun(int v) { return v == V_XPFUN || v == V_XNPFUN || v == V_YPFUN || v == V_YNPFUN ||
                                            v == V_XYPFUN || v == V_XYNPFUN; }
 __host__ __device__ inline bool variant_is_periodic(int v) { return v == V_XP || v == V_XPFUN || v == V_YP || v == V_YPFUN ||
-                                                v == V_XYP || v == V_XYPFUN; }
+                                                v == V_XYP || v == V_XYPFUN || v == V_XYWENOADVP; }
 __host__ __device__ inline int variant_dir(int v) { return v < 4 ? 0 : (v < 8 ? 1 : 2); }   // 0 = X, 1 = Y, 2 = XY
 
 // Per-point outcome of one Compute.
@@ -50,6 +51,10 @@ struct StencilArgs {
     int wrap_x;           // 1: columns outside [0,nx) wrap around (periodic variants)
     int has_top, has_bot; // 1: halo rows above / below may be read
     int vec_ok;           // 1: rows are 16-byte aligned, vector loads/stores allowed
+    // WENO advection only: velocity rows row0.. and the inverse grid spacings (coeDx, coeDy)
+    const void* u;
+    const void* v;
+    double cdx, cdy;
 };
 
 // Write rule of the reference for point (x, gy) of the field, gy a field row.
@@ -140,5 +145,6 @@ constexpr uint32_t kPlanMagic = 0xC5E7B300u;
 // *path is set to 1 when the TMA-staged kernel ran, 0 for the plain-load kernel.
 cudaError_t launch_stencil_f64(const StencilArgs& a, cudaStream_t s, int* path);
 cudaError_t launch_stencil_f32(const StencilArgs& a, cudaStream_t s, int* path);
+cudaError_t launch_weno_adv(const StencilArgs& a, cudaStream_t s);
 
 }  // namespace custen

@@ -107,7 +107,7 @@ int create_plan(cuSten_t* h, int variant, int dtype, int dev, int numTiles, int 
                 void* out, void* in, void* coef, int H, int L, int R, int V, int T, int B, int ncoef, void* func,
                 int numStenField) {
     if (h == nullptr) return fail_arg("cuSten handle is NULL");
-    if (variant < 0 || variant >= V_COUNT) return fail_arg("unknown stencil variant %d", variant);
+    if (variant < 0 || variant > V_XYWENOADVP) return fail_arg("unknown stencil variant %d", variant);
     if (dtype != DT_F64 && dtype != DT_F32) return fail_arg("unknown data type %d", dtype);
     if (numTiles < 1) return fail_arg("numTiles must be >= 1 (got %d)", numTiles);
     if (nx < 1 || ny < 1) return fail_arg("nx and ny must be >= 1 (got %d x %d)", nx, ny);
@@ -218,6 +218,35 @@ int create_plan(cuSten_t* h, int variant, int dtype, int dev, int numTiles, int 
     return ST_OK;
 }
 
+// cuStenCreate2DXYWENOADVp (custenCreateDestroy2DXYADVWENOp.cu:57-257): a 7 x 7 window (L = R = T =
+// B = 3), coeDx = 1/dx, coeDy = 1/dy, per-tile input / output / velocity pointers and periodic halo
+// pointers. The reference's kernel also assumes nx % BLOCK_X == 0, nyTile % BLOCK_Y == 0 and at least two
+// blocks per direction; this library computes the periodic operator for any nx and any nyTile >= 3.
+int create_weno_plan(cuSten_t* h, int dev, int numTiles, int nx, int ny, int BX, int BY, double dx, double dy,
+                     double* u, double* v, double* out, double* in) {
+    if (h == nullptr) return fail_arg("cuSten handle is NULL");
+    if (u == nullptr || v == nullptr) return fail_arg("velocity pointers must not be NULL");
+    if (!(dx != 0.0) || !(dy != 0.0)) return fail_arg("grid spacings must be non-zero");
+    if (numTiles >= 1 && ny % numTiles == 0 && ny / numTiles < 3)
+        return fail_arg("WENO needs at least 3 rows per tile (ny=%d numTiles=%d)", ny, numTiles);
+    int st = create_plan(h, V_XYWENOADVP, DT_F64, dev, numTiles, nx, ny, BX, BY, out, in, nullptr, 7, 3, 3, 7, 3, 3,
+                         0, nullptr, 49);
+    if (st != ST_OK) return st;
+    h->coeDx = 1.0 / dx;
+    h->coeDy = 1.0 / dy;
+    h->numStenHoriz = 7;
+    h->numStenVert = 7;
+    h->mem_shared = (int)(((size_t)h->nxLocal * h->nyLocal + 49) * sizeof(double));
+    const size_t tile_elems = (size_t)nx * h->nyTile;
+    h->uVel = static_cast<double**>(malloc(numTiles * sizeof(double*)));
+    h->vVel = static_cast<double**>(malloc(numTiles * sizeof(double*)));
+    for (int t = 0; t < numTiles; ++t) {
+        h->uVel[t] = u + t * tile_elems;
+        h->vVel[t] = v + t * tile_elems;
+    }
+    return ST_OK;
+}
+
 static int destroy_plan(cuSten_t* h) {
     PlanPrivate* p = priv_of(h);
     if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
@@ -245,6 +274,9 @@ static int destroy_plan(cuSten_t* h) {
     free(h->dataOutput);
     free(h->boundaryTop);
     free(h->boundaryBottom);
+    free(h->uVel);
+    free(h->vVel);
+    h->uVel = h->vVel = nullptr;
     h->streams = nullptr;
     h->events = nullptr;
     h->dataInput = h->dataOutput = h->boundaryTop = h->boundaryBottom = nullptr;
@@ -300,7 +332,9 @@ static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 
 static cudaError_t launch(const StencilArgs& a, int dtype, cudaStream_t s, PlanPrivate* p) {
     int path = 0;
-    cudaError_t e = dtype == DT_F64 ? launch_stencil_f64(a, s, &path) : launch_stencil_f32(a, s, &path);
+    cudaError_t e = a.variant == V_XYWENOADVP ? launch_weno_adv(a, s)
+                    : dtype == DT_F64        ? launch_stencil_f64(a, s, &path)
+                                             : launch_stencil_f32(a, s, &path);
     if (e == cudaSuccess) {
         ++p->launches;
         g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -364,7 +398,8 @@ static int compute_staged(cuSten_t* h, PlanPrivate* p, StencilArgs& a, cudaStrea
         rows = std::min(rows, nyT);
         const size_t in_bytes = align256((size_t)(T + rows + B) * row_bytes);
         const size_t out_bytes = align256((size_t)rows * row_bytes);
-        const size_t slot = in_bytes + out_bytes;
+        // WENO advection also streams its two velocity fields
+        const size_t slot = in_bytes + out_bytes * (p->variant == V_XYWENOADVP ? 3 : 1);
         const size_t coef_bytes = align256((size_t)std::max(p->ncoef, 1) * esz);
         CU_TRY(cudaMalloc(&p->stage, kStageSlots * slot + coef_bytes), "Allocating staging buffers");
         p->stage_slot_bytes = slot;
@@ -385,7 +420,7 @@ static int compute_staged(cuSten_t* h, PlanPrivate* p, StencilArgs& a, cudaStrea
     // Weights (or Fun coefficients) once per Compute: the kernels then read device memory only.
     // The copy waits for every kernel of the previous Compute that may still read the old ones.
     for (int k = 0; k < kStageSlots; ++k) CU_TRY(cudaStreamWaitEvent(s_in, p->stage_ev[3 * k + 1], 0), "Ordering");
-    if (p->ncoef > 0) {
+    if (p->ncoef > 0 && a.coef != nullptr) {
         CU_TRY(cudaMemcpyAsync(coef_dev, a.coef, (size_t)p->ncoef * esz, cudaMemcpyDefault, s_in), "Copying weights");
         h2d += (size_t)p->ncoef * esz;
         a.coef = coef_dev;
@@ -399,6 +434,8 @@ static int compute_staged(cuSten_t* h, PlanPrivate* p, StencilArgs& a, cudaStrea
             cudaEvent_t ev_in = p->stage_ev[3 * k], ev_kern = p->stage_ev[3 * k + 1], ev_out = p->stage_ev[3 * k + 2];
             char* in_slot = stage + (size_t)k * slot_bytes;
             char* out_slot = in_slot + in_bytes;
+            char* u_slot = out_slot + align256((size_t)rows * row_bytes);
+            char* v_slot = u_slot + align256((size_t)rows * row_bytes);
             const int gy0 = t * nyT + r0;
             const bool has_top = dir != 0 && T > 0 && (periodic || gy0 > 0);
             const bool has_bot = dir != 0 && B > 0 && (periodic || gy0 + rc < ny);
@@ -438,6 +475,16 @@ static int compute_staged(cuSten_t* h, PlanPrivate* p, StencilArgs& a, cudaStrea
                         h2d += (size_t)wl * esz * rc;
                     }
                 }
+            }
+            if (p->variant == V_XYWENOADVP) {
+                const size_t off = (size_t)r0 * row_bytes, bytes = (size_t)rc * row_bytes;
+                CU_TRY(cudaMemcpyAsync(u_slot, byte_ptr(h->uVel[t]) + off, bytes, cudaMemcpyDefault, s_in),
+                       "Copying velocity rows to the device");
+                CU_TRY(cudaMemcpyAsync(v_slot, byte_ptr(h->vVel[t]) + off, bytes, cudaMemcpyDefault, s_in),
+                       "Copying velocity rows to the device");
+                h2d += 2 * bytes;
+                a.u = u_slot;
+                a.v = v_slot;
             }
             CU_TRY(cudaEventRecord(ev_in, s_in), "Recording event");
             CU_TRY(cudaStreamWaitEvent(s_comp, ev_in, 0), "Ordering kernel after copy-in");
@@ -494,14 +541,24 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
     a.nyTile = nyT;
     a.numTiles = nt;
     a.wrap_x = periodic && dir != 1;
+    if (p->variant == V_XYWENOADVP) {
+        // the reference passes coeDx / coeDy from the handle at every Compute (2d_xyADVWENO_p_kernel.cu:479-480)
+        a.cdx = h->coeDx;
+        a.cdy = h->coeDy;
+        a.coef = nullptr;
+    }
 
     // Tiles contiguous and every interior halo pointer naming the neighbouring rows of that array?
     char* in0 = byte_ptr(h->dataInput[0]);
     char* out0 = byte_ptr(h->dataOutput[0]);
+    const bool weno = p->variant == V_XYWENOADVP;
     bool contiguous = true;
     for (int t = 0; t < nt && contiguous; ++t) {
         if (byte_ptr(h->dataInput[t]) != in0 + t * tile_bytes) contiguous = false;
         if (byte_ptr(h->dataOutput[t]) != out0 + t * tile_bytes) contiguous = false;
+        if (weno && (byte_ptr(h->uVel[t]) != byte_ptr(h->uVel[0]) + t * tile_bytes ||
+                     byte_ptr(h->vVel[t]) != byte_ptr(h->vVel[0]) + t * tile_bytes))
+            contiguous = false;
         if (dir != 0 && contiguous) {
             if (t > 0 && p->T > 0 &&
                 byte_ptr(h->boundaryTop[t]) != in0 + ((long)t * nyT - p->T) * (long)nx * esz)
@@ -519,6 +576,10 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
     auto fill_launch = [&](int t_first, int t_count) {
         a.in = h->dataInput[t_first];
         a.out = h->dataOutput[t_first];
+        if (weno) {
+            a.u = h->uVel[t_first];
+            a.v = h->vVel[t_first];
+        }
         a.rows = t_count * nyT;
         a.row0 = t_first * nyT;
         const int t_last = t_first + t_count - 1;
@@ -562,6 +623,9 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
         moved_in += 2 * tile_bytes + (dir != 0 ? halo_top_bytes + halo_bot_bytes : 0);
         cudaError_t e = prefetch(h->dataInput[t], tile_bytes, dev, copy_s);
         if (e == cudaSuccess) e = prefetch(h->dataOutput[t], tile_bytes, dev, copy_s);
+        if (e == cudaSuccess && weno) e = prefetch(h->uVel[t], tile_bytes, dev, copy_s);
+        if (e == cudaSuccess && weno) e = prefetch(h->vVel[t], tile_bytes, dev, copy_s);
+        if (weno) moved_in += 2 * tile_bytes;
         if (e == cudaSuccess && dir != 0 && halo_top_bytes) e = prefetch(h->boundaryTop[t], halo_top_bytes, dev, copy_s);
         if (e == cudaSuccess && dir != 0 && halo_bot_bytes) e = prefetch(h->boundaryBottom[t], halo_bot_bytes, dev, copy_s);
         if (e == cudaSuccess) e = cudaEventRecord(h->events[t & 1], copy_s);
@@ -576,6 +640,11 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
             moved_out += 2 * tile_bytes;
             CU_TRY(prefetch(h->dataOutput[t], tile_bytes, -1, s), "Offloading output tile");
             CU_TRY(prefetch(h->dataInput[t], tile_bytes, -1, s), "Offloading input tile");
+            if (weno) {
+                moved_out += 2 * tile_bytes;
+                CU_TRY(prefetch(h->uVel[t], tile_bytes, -1, s), "Offloading velocity tile");
+                CU_TRY(prefetch(h->vVel[t], tile_bytes, -1, s), "Offloading velocity tile");
+            }
         }
         if (t + 1 < nt) CU_TRY(prefetch_tile(t + 1), "Prefetching tile");
     }
@@ -695,6 +764,13 @@ CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYp)
 CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYnp)
 CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYpFun)
 CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYnpFun)
+CUSTEN_DEFINE_SWAP_DESTROY_COMPUTE(XYWENOADVp)
+
+// ---- XY WENO advection, periodic (cuSten_struct_functions.h:290-347, stencil_kernels.h:181-189) ----
+void cuStenCreate2DXYWENOADVp(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double dx, double dy,
+                              double* u, double* v, double* out, double* in) {
+    exit_on(create_weno_plan(h, dev, nt, nx, ny, bx, by, dx, dy, u, v, out, in));
+}
 
 // The reference library defines the XpFun compute under this misspelt name (2d_x_p_fun_kernel.cu:172).
 void cuSenCompute2DXpFun(cuSten_t* h, bool offload) { exit_on(compute_plan(h, offload ? 1 : 0, nullptr)); }
@@ -717,6 +793,8 @@ void custen_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h) {
 
 int custen_create(cuSten_t* h, int variant, int dtype, int dev, int nt, int nx, int ny, int bx, int by, void* out,
                   void* in, void* coef, int H, int L, int R, int V, int T, int B, int ncoef, void* func) {
+    if (variant == V_XYWENOADVP)
+        return fail_arg("the WENO advection stencil is created with custen_create_2d_xyweno_adv_p");
     const int dir = (variant >= 0 && variant < V_COUNT) ? variant_dir(variant) : 0;
     const int field = dir == 2 ? H * V : (dir == 0 ? H : V);
     return create_plan(h, variant, dtype, dev, nt, nx, ny, bx, by, out, in, coef, H, L, R, V, T, B, ncoef, func,
@@ -803,6 +881,11 @@ int custen_create_2d_xynp_fun(cuSten_t* h, int dev, int nt, int nx, int ny, int 
                               double* in, double* coe, int Hs, int L, int R, int Vs, int T, int B, double* func) {
     return create_plan(h, V_XYNPFUN, DT_F64, dev, nt, nx, ny, bx, by, out, in, coe, Hs, L, R, Vs, T, B, Hs * Vs,
                        func, Hs * Vs);
+}
+
+int custen_create_2d_xyweno_adv_p(cuSten_t* h, int dev, int nt, int nx, int ny, int bx, int by, double dx, double dy,
+                                  double* u, double* v, double* out, double* in) {
+    return create_weno_plan(h, dev, nt, nx, ny, bx, by, dx, dy, u, v, out, in);
 }
 
 int custen_device_error(unsigned int* flags, int clear) {

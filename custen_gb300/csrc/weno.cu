@@ -1,0 +1,150 @@
+// WENO5 advection stencil, periodic in x and y (the thirteenth cuSten operator,
+// cuSten/src/kernels/2d_xyADVWENO_p_kernel.cu), for sm_103a.
+//
+// out[y][x] = u[y][x] * Fx + v[y][x] * Fy, where Fx (Fy) is the fifth-order WENO reconstruction of the
+// upwind one-sided differences D[i] = (in[i] - in[i-1]) * coeDx along x (along y with coeDy): for u > 0
+// the differences at x-2 .. x+2, otherwise those at x+3 .. x-1 in reverse order (the reference's
+// upwind selection, 2d_xyADVWENO_p_kernel.cu:286-348 and :352-414).
+//
+// GB300 shape: about 200 FP64 operations per point (eight correctly rounded divisions among them)
+// against 32 bytes of compulsory traffic, so the FP64 pipe bounds this operator by a wide margin.
+// The kernel therefore spends no FP64 work twice: a 64 x 32 tile with its 3-point periodic halo is
+// staged once, and the x and y differences are formed once per tile into shared memory (the
+// reference forms five differences per point and direction). The reconstruction keeps the reference's
+// operation order, including its single-precision powf on the smoothness terms, so that results are
+// bit-identical to the reference's kernel on the same GPU.
+#include <cuda_runtime.h>
+
+#include "custen_internal.h"
+
+namespace custen {
+namespace {
+
+constexpr int kWenoTW = 64;                 // tile columns (one per thread column)
+constexpr int kWenoTH = 32;                 // tile rows
+constexpr int kWenoHalo = 3;                // i-3 .. i+3
+constexpr int kWenoThreads = 256;           // 64 columns x 4 thread rows
+constexpr int kWenoSW = kWenoTW + 2 * kWenoHalo;   // 70 staged columns
+constexpr int kWenoSH = kWenoTH + 2 * kWenoHalo;   // 38 staged rows
+constexpr int kWenoDXW = kWenoTW + 5;       // x differences at columns x0-2 .. x0+TW+2
+constexpr int kWenoDYH = kWenoTH + 5;       // y differences at rows y0-2 .. y0+TH+2
+constexpr size_t kWenoSmem = sizeof(double) * ((size_t)kWenoSH * kWenoSW + (size_t)kWenoTH * kWenoDXW +
+                                               (size_t)kWenoDYH * kWenoTW);
+
+// Fifth-order WENO reconstruction (Jiang & Shu 1996, in the notation of Osher & Fedkiw, "Level Set
+// Methods and Dynamic Implicit Surfaces", 3.4) from five consecutive differences a..e. The three
+// candidate stencils, the smoothness indicators and the nonlinear weights are evaluated in the order
+// of the reference's wenoSten (2d_xyADVWENO_p_kernel.cu:52-88): same expressions, same contraction,
+// and the smoothness squares and the squared (indicator + 1e-6) taken by powf in single precision.
+__device__ __forceinline__ double weno5(double a, double b, double c, double d, double e) {
+    const double q1 = (1.0 / 3.0) * a - (7.0 / 6.0) * b + (11.0 / 6.0) * c;
+    const double q2 = -(1.0 / 6.0) * b + (5.0 / 6.0) * c + (1.0 / 3.0) * d;
+    const double q3 = (1.0 / 3.0) * c + (5.0 / 6.0) * d - (1.0 / 6.0) * e;
+
+    const double is1 = (13.0 / 12.0) * powf((float)(a - 2.0 * b + c), 2.0f) +
+                       0.25 * powf((float)(a - 4.0 * b + 3.0 * c), 2.0f);
+    const double is2 = (13.0 / 12.0) * powf((float)(b - 2.0 * c + d), 2.0f) + 0.25 * powf((float)(b - d), 2.0f);
+    const double is3 = (13.0 / 12.0) * powf((float)(c - 2.0 * d + e), 2.0f) +
+                       0.25 * powf((float)(3.0 * c - 4.0 * d + e), 2.0f);
+
+    const double eps = 1e-06;
+    const double g1 = 0.1 / powf((float)(is1 + eps), 2.0f);
+    const double g2 = 0.6 / powf((float)(is2 + eps), 2.0f);
+    const double g3 = 0.3 / powf((float)(is3 + eps), 2.0f);
+    const double norm = 1.0 / (g1 + g2 + g3);
+    const double w1 = g1 * norm, w2 = g2 * norm, w3 = g3 * norm;
+    return q1 * w1 + q2 * w2 + q3 * w3;
+}
+
+__device__ __forceinline__ int wrap_col(int c, int nx) {
+    c %= nx;
+    return c < 0 ? c + nx : c;
+}
+
+// One CTA per 64 x 32 tile of the launch's rows. Rows above / below the launch come from the T = 3
+// halo rows at `top` / `bot` (the handle's boundaryTop/boundaryBottom of the tile, periodic); columns
+// wrap around the field.
+__global__ void __launch_bounds__(kWenoThreads, 2) weno_adv_kernel(double* __restrict__ out,
+                                                                   const double* __restrict__ in,
+                                                                   const double* __restrict__ uvel,
+                                                                   const double* __restrict__ vvel,
+                                                                   const double* __restrict__ top,
+                                                                   const double* __restrict__ bot, double cdx,
+                                                                   double cdy, int nx, int rows) {
+    extern __shared__ __align__(16) double wsm[];
+    double* tile = wsm;                                   // [SH][SW]
+    double* dxs = tile + kWenoSH * kWenoSW;               // [TH][DXW]
+    double* dys = dxs + kWenoTH * kWenoDXW;               // [DYH][TW]
+    const int x0 = blockIdx.x * kWenoTW, y0 = blockIdx.y * kWenoTH;
+    const int tid = threadIdx.x;
+
+    // stage the tile and its halo: staged (r, c) is field row y0-3+r, column x0-3+c (wrapped)
+    for (int e = tid; e < kWenoSH * kWenoSW; e += kWenoThreads) {
+        const int r = e / kWenoSW, c = e - r * kWenoSW;
+        const int gy = y0 - kWenoHalo + r;
+        const int gx = wrap_col(x0 - kWenoHalo + c, nx);
+        double val = 0.0;
+        if (gy < 0) val = top[(size_t)(gy + kWenoHalo) * nx + gx];
+        else if (gy < rows) val = in[(size_t)gy * nx + gx];
+        else if (gy < rows + kWenoHalo) val = bot[(size_t)(gy - rows) * nx + gx];
+        tile[e] = val;
+    }
+    __syncthreads();
+    // differences, each formed once: D(i) = (f[i] - f[i-1]) * coe (2d_xyADVWENO_p_kernel.cu:290-309)
+    for (int e = tid; e < kWenoTH * kWenoDXW; e += kWenoThreads) {
+        const int r = e / kWenoDXW, c = e - r * kWenoDXW;
+        const double* row = tile + (r + kWenoHalo) * kWenoSW;
+        dxs[e] = (row[c + 1] - row[c]) * cdx;
+    }
+    for (int e = tid; e < kWenoDYH * kWenoTW; e += kWenoThreads) {
+        const int r = e / kWenoTW, c = e - r * kWenoTW;
+        dys[e] = (tile[(r + 1) * kWenoSW + c + kWenoHalo] - tile[r * kWenoSW + c + kWenoHalo]) * cdy;
+    }
+    __syncthreads();
+
+    const int tx = tid % kWenoTW;
+    const int x = x0 + tx;
+    if (x >= nx) return;
+    for (int ty = tid / kWenoTW; ty < kWenoTH; ty += kWenoThreads / kWenoTW) {
+        const int y = y0 + ty;
+        if (y >= rows) break;
+        const size_t q = (size_t)y * nx + x;
+        const double uu = uvel[q], vv = vvel[q];
+        // Upwind side: the five differences are selected first and reconstructed once (two calls in a
+        // conditional expression would let the compiler evaluate both and double the FP64 work).
+        const double* dr = dxs + ty * kWenoDXW + tx;      // dr[k] = D at column x - 2 + k
+        const bool ux = uu > 0.0;
+        const double fx = weno5(ux ? dr[0] : dr[5], ux ? dr[1] : dr[4], dr[2 + !ux], ux ? dr[3] : dr[2],
+                                ux ? dr[4] : dr[1]);
+        const double* dc = dys + ty * kWenoTW + tx;       // dc[k * TW] = D at row y - 2 + k
+        const bool vy = vv > 0.0;
+        const double fy = weno5(vy ? dc[0] : dc[5 * kWenoTW], vy ? dc[kWenoTW] : dc[4 * kWenoTW],
+                                dc[(2 + !vy) * kWenoTW], vy ? dc[3 * kWenoTW] : dc[2 * kWenoTW],
+                                vy ? dc[4 * kWenoTW] : dc[kWenoTW]);
+        // (2d_xyADVWENO_p_kernel.cu:424)
+        out[q] = uu * fx + vv * fy;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_weno_adv(const StencilArgs& a, cudaStream_t s) {
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+        e = cudaFuncSetAttribute(weno_adv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWenoSmem);
+        if (e != cudaSuccess) return e;
+        attr_set[dev] = true;
+    }
+    if (a.rows <= 0 || a.nx <= 0) return cudaSuccess;
+    dim3 grid((a.nx + kWenoTW - 1) / kWenoTW, (a.rows + kWenoTH - 1) / kWenoTH);
+    weno_adv_kernel<<<grid, kWenoThreads, kWenoSmem, s>>>(
+        static_cast<double*>(a.out), static_cast<const double*>(a.in), static_cast<const double*>(a.u),
+        static_cast<const double*>(a.v), static_cast<const double*>(a.top), static_cast<const double*>(a.bot),
+        a.cdx, a.cdy, a.nx, a.rows);
+    return cudaGetLastError();
+}
+
+}  // namespace custen

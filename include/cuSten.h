@@ -164,6 +164,15 @@ void cuStenCreate2DYpFun(cuSten_t* pt_cuSten, int deviceNum, int numTiles, int n
 void cuStenSwap2DYpFun(cuSten_t* pt_cuSten, double* dataInput);
 void cuStenDestroy2DYpFun(cuSten_t* pt_cuSten);
 
+/* ---- 2D xy direction, periodic WENO advection (:290-347) ----
+ * out = u * WENO5_x(in) + v * WENO5_y(in), upwinded on the signs of u and v; coeDx = 1/dx and
+ * coeDy = 1/dy are stored in the handle. */
+void cuStenCreate2DXYWENOADVp(cuSten_t* pt_cuSten, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X,
+                              int BLOCK_Y, double dx, double dy, double* u, double* v, double* dataOutput,
+                              double* dataInput);
+void cuStenSwap2DXYWENOADVp(cuSten_t* pt_cuSten, double* dataInput);
+void cuStenDestroy2DXYWENOADVp(cuSten_t* pt_cuSten);
+
 /* ---- Compute (cuSten/src/kernels/stencil_kernels.h:52-189) ---- */
 void cuStenCompute2DXnp(cuSten_t* pt_cuSten, bool offload);
 void cuStenCompute2DXnpFun(cuSten_t* pt_cuSten, bool offload);
@@ -180,5 +189,6 @@ void cuStenCompute2DXYp(cuSten_t* pt_cuSten, bool offload);
 void cuStenCompute2DXYpFun(cuSten_t* pt_cuSten, bool offload);
 void cuStenCompute2DXYnp(cuSten_t* pt_cuSten, bool offload);
 void cuStenCompute2DXYnpFun(cuSten_t* pt_cuSten, bool offload);
+void cuStenCompute2DXYWENOADVp(cuSten_t* pt_cuSten, bool offload);
 
 #endif /* CUSTEN_H */

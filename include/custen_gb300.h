@@ -27,7 +27,8 @@ extern "C" {
 enum {
     CUSTEN_XP = 0, CUSTEN_XNP = 1, CUSTEN_XPFUN = 2, CUSTEN_XNPFUN = 3,
     CUSTEN_YP = 4, CUSTEN_YNP = 5, CUSTEN_YPFUN = 6, CUSTEN_YNPFUN = 7,
-    CUSTEN_XYP = 8, CUSTEN_XYNP = 9, CUSTEN_XYPFUN = 10, CUSTEN_XYNPFUN = 11
+    CUSTEN_XYP = 8, CUSTEN_XYNP = 9, CUSTEN_XYPFUN = 10, CUSTEN_XYNPFUN = 11,
+    CUSTEN_XYWENOADVP = 12   /* created by custen_create_2d_xyweno_adv_p only */
 };
 enum { CUSTEN_F64 = 0, CUSTEN_F32 = 1 };
 
@@ -106,6 +107,13 @@ int custen_create_2d_xyp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, i
 int custen_create_2d_xynp_fun(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X, int BLOCK_Y,
                               double* dataOutput, double* dataInput, double* coe, int numStenHoriz, int numStenLeft,
                               int numStenRight, int numStenVert, int numStenTop, int numStenBottom, double* func);
+
+/* WENO5 advection, periodic: cuStenCreate2DXYWENOADVp (cuSten_struct_functions.h:290-324); computed by
+ * custen_compute like every other handle (cuStenCompute2DXYWENOADVp, stencil_kernels.h:181-189), swapped
+ * with custen_swap, destroyed with custen_destroy. */
+int custen_create_2d_xyweno_adv_p(cuSten_t* h, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X,
+                                  int BLOCK_Y, double dx, double dy, double* u, double* v, double* dataOutput,
+                                  double* dataInput);
 
 /* ---- device functions shipped with the library for the Fun variants ----
  * id 0: X  (d[l-1] - 2 d[l] + d[l+1]) * coe[0]

@@ -3,6 +3,8 @@ baseline leg as the checker; never by the library).
 
 * ``stencil_oracle.c``: C restatement of the twelve cuSten stencil kernels (block-by-block emulation,
   see the header of that file).
+* ``weno_oracle.c``: C restatement of the periodic WENO5 advection operator
+  (cuSten/src/kernels/2d_xyADVWENO_p_kernel.cu).
 * ``ch_oracle.c``: C restatement of the Cahn-Hilliard ADI solver of
   cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c.
 * ``ref_build.py``: builds the reference's own code from the reference sources into ``oracle/_ref``
@@ -21,7 +23,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "liboracle.so"
-SOURCES = [HERE / "stencil_oracle.c", HERE / "ch_oracle.c"]
+SOURCES = [HERE / "stencil_oracle.c", HERE / "ch_oracle.c", HERE / "weno_oracle.c"]
 HEADERS = [HERE / "stencil_oracle_impl.h"]
 
 REFRUN = BUILD / "librefrun.so"
@@ -74,6 +76,8 @@ def lib() -> ctypes.CDLL:
             f.restype = i
         L.oracle_host_loop_xyp_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i]
         L.oracle_host_loop_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i, i]
+        L.oracle_weno_f64.argtypes = [i, i, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double]
+        L.oracle_weno_f64.restype = None
         L.ch_oracle_create.argtypes = [i, ctypes.c_double, vp]
         L.ch_oracle_create.restype = vp
         L.ch_oracle_step.argtypes = [vp, i]
@@ -105,6 +109,16 @@ def stencil(variant: int, out: np.ndarray, inp: np.ndarray, coef: np.ndarray, *,
     if rc != 0:
         raise ValueError("configuration outside the reference kernels' contract")
     return status
+
+
+def weno(inp: np.ndarray, u: np.ndarray, v: np.ndarray, cdx: float, cdy: float) -> np.ndarray:
+    """Periodic WENO5 advection, out = u * Fx + v * Fy (weno_oracle.c); cdx = 1/dx, cdy = 1/dy."""
+    inp, u, v = (np.ascontiguousarray(a, dtype=np.float64) for a in (inp, u, v))
+    ny, nx = inp.shape
+    out = np.empty_like(inp)
+    lib().oracle_weno_f64(nx, ny, inp.ctypes.data, u.ctypes.data, v.ctypes.data, out.ctypes.data, float(cdx),
+                          float(cdy))
+    return out
 
 
 def host_loop_xyp(inp: np.ndarray, w: np.ndarray, H: int, L: int, V: int, T: int, y0: int = 0,
@@ -194,6 +208,7 @@ def reference_kernels():
         R.refrun_load.argtypes = [ctypes.c_char_p]
         R.refrun_fun_ptr.argtypes = [i, ctypes.POINTER(ctypes.c_ulonglong)]
         R.refrun_compute.argtypes = [i, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, i, ctypes.c_ulonglong]
+        R.refrun_weno.argtypes = [i, i, i, i, i, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double]
         if R.refrun_load(str(REF_CUBIN).encode()) != 0:
             raise RuntimeError(R.refrun_error().decode())
         _refrun = R
@@ -215,5 +230,14 @@ def reference_compute(variant: int, nx: int, ny: int, num_tiles: int, bx: int, b
     Rr = reference_kernels()
     rc = Rr.refrun_compute(variant, nx, ny, num_tiles, bx, by, out_ptr, in_ptr, halo_ptr or in_ptr, coef_ptr,
                            num_sten, H, L, R, V, T, B, num_coe, func)
+    if rc != 0:
+        raise RuntimeError(Rr.refrun_error().decode())
+
+
+def reference_weno(nx: int, ny: int, num_tiles: int, bx: int, by: int, out_ptr: int, in_ptr: int, u_ptr: int,
+                   v_ptr: int, cdx: float, cdy: float) -> None:
+    """One Compute of the reference's WENO advection kernel on device buffers (device pointers)."""
+    Rr = reference_kernels()
+    rc = Rr.refrun_weno(nx, ny, num_tiles, bx, by, out_ptr, in_ptr, u_ptr, v_ptr, float(cdx), float(cdy))
     if rc != 0:
         raise RuntimeError(Rr.refrun_error().decode())

@@ -1,4 +1,4 @@
-// Compiles the reference cuSten kernels, unchanged, from the reference sources into one sm_103a
+// Compiles the reference cuSten kernels (the twelve stencils and the WENO advection), unchanged, from the reference sources into one sm_103a
 // cubin (oracle/_ref/custen_ref_sm103a.cubin) -- TEST INFRASTRUCTURE ONLY. Built by
 // oracle/ref_build.py where the reference sources exist (REF_ROOT); driven by oracle/ref_runner.cpp.
 // The user functions are the library's shipped Fun functions (custen_gb300/csrc/builtin_funs.cuh),
@@ -18,6 +18,7 @@
 #include CUSTEN_REF_KERNEL(2d_xy_np_kernel.cu)
 #include CUSTEN_REF_KERNEL(2d_xy_p_fun_kernel.cu)
 #include CUSTEN_REF_KERNEL(2d_xy_np_fun_kernel.cu)
+#include CUSTEN_REF_KERNEL(2d_xyADVWENO_p_kernel.cu)
 
 typedef double (*RefFx)(double*, double*, int);
 typedef double (*RefFy)(double*, double*, int, int);

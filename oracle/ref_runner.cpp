@@ -19,6 +19,7 @@ namespace {
 
 CUmodule g_mod = nullptr;
 CUfunction g_kern[12] = {};
+CUfunction g_weno = nullptr;   // kernel2DXYWENOADVp
 const char* kNames[12] = {"kernel2DXp", "kernel2DXnp", "kernel2DXpFun", "kernel2DXnpFun",
                           "kernel2DYp", "kernel2DYnp", "kernel2DYpFun", "kernel2DYnpFun",
                           "kernel2DXYp", "kernel2DXYnp", "kernel2DXYpFun", "kernel2DXYnpFun"};
@@ -66,6 +67,7 @@ int refrun_load(const char* cubin) {
         std::string b = base_name(nm);
         for (int k = 0; k < 12; ++k)
             if (b == kNames[k]) g_kern[k] = fs[i];
+        if (b == "kernel2DXYWENOADVp") g_weno = fs[i];
     }
     for (int k = 0; k < 12; ++k)
         if (!g_kern[k]) {
@@ -169,6 +171,42 @@ int refrun_compute(int variant, int nx, int ny, int numTiles, int BX, int BY, do
             break;
         }
         CUresult r = cuLaunchKernel(k, nx / BX, nyTile / BY, 1, BX, BY, 1, (unsigned)smem, nullptr, args, nullptr);
+        if (r != CUDA_SUCCESS) return fail(r, "cuLaunchKernel");
+    }
+    CUresult r = cuCtxSynchronize();
+    if (r != CUDA_SUCCESS) return fail(r, "cuCtxSynchronize");
+    return 0;
+}
+
+// One reference Compute of the WENO advection operator (cuStenCompute2DXYWENOADVp,
+// 2d_xyADVWENO_p_kernel.cu:440-548): per tile, grid (nx/BLOCK_X, nyTile/BLOCK_Y), shared memory
+// (nxLocal*nyLocal + 49) doubles with nxLocal = BLOCK_X + 6, nyLocal = BLOCK_Y + 6
+// (custenCreateDestroy2DXYADVWENOp.cu:149-156), the periodic halo pointers of its Create (:206-243).
+int refrun_weno(int nx, int ny, int numTiles, int BX, int BY, double* out, double* in, double* u, double* v,
+                double cdx, double cdy) {
+    if (!g_mod || !g_weno) {
+        snprintf(g_err, sizeof(g_err), "reference WENO kernel not loaded");
+        return 1;
+    }
+    const int nyTile = ny / numTiles;
+    int numSten = 49, H = 7, L = 3, R = 3, V = 7, T = 3, B = 3;
+    int nxLocal = BX + 6, nyLocal = BY + 6;
+    const size_t smem = ((size_t)nxLocal * nyLocal + 49) * sizeof(double);
+    if (smem > 48 * 1024) {
+        CUresult r = cuFuncSetAttribute(g_weno, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem);
+        if (r != CUDA_SUCCESS) return fail(r, "cuFuncSetAttribute");
+    }
+    for (int t = 0; t < numTiles; ++t) {
+        const size_t off = (size_t)t * nyTile * nx;
+        double* o = out + off;
+        double* i = in + off;
+        double* uu = u + off;
+        double* vv = v + off;
+        double* btop = in + (size_t)((t == 0) ? (ny - T) : (t * nyTile - T)) * nx;
+        double* bbot = in + (size_t)((t == numTiles - 1) ? 0 : (t + 1) * nyTile) * nx;
+        void* args[] = {&o, &i, &uu, &vv, &btop, &bbot, &cdx, &cdy, &numSten, &H, &L, &R, &V, &T, &B,
+                        &nxLocal, &nyLocal, &BX, &BY, &nx, (void*)&nyTile};
+        CUresult r = cuLaunchKernel(g_weno, nx / BX, nyTile / BY, 1, BX, BY, 1, (unsigned)smem, nullptr, args, nullptr);
         if (r != CUDA_SUCCESS) return fail(r, "cuLaunchKernel");
     }
     CUresult r = cuCtxSynchronize();

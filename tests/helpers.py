@@ -107,3 +107,17 @@ def weights_for(variant: int, H: int, V: int, seed: int, dtype=np.float64, zeros
 def sentinel(nx: int, ny: int, dtype=np.float64) -> np.ndarray:
     """Pre-fill of the output: distinct, finite, recognisable values."""
     return (np.arange(nx * ny, dtype=np.float64).reshape(ny, nx) * 1e-3 + 12345.0).astype(dtype)
+
+
+def weno_inputs(nx: int, ny: int, seed: int, rough: bool = False):
+    """Advected field, velocities and spacings for the WENO operator: the benchmark field (or, rough,
+    a random one that drives the nonlinear weights), u and v of both signs with some exact zeros (the
+    reference's `> 0.0` test sends them to the other upwind side), dx = 2 pi / nx, dy = 2 pi / ny."""
+    rng = np.random.default_rng(500 + seed)
+    f = rng.standard_normal((ny, nx)) if rough else field(nx, ny, seed)
+    u = rng.uniform(-1.0, 1.0, (ny, nx))
+    v = rng.uniform(-1.0, 1.0, (ny, nx))
+    u[rng.random((ny, nx)) < 0.05] = 0.0
+    v[rng.random((ny, nx)) < 0.05] = 0.0
+    return (np.ascontiguousarray(f), np.ascontiguousarray(u), np.ascontiguousarray(v), 2 * np.pi / nx,
+            2 * np.pi / ny)

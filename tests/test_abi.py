@@ -31,6 +31,8 @@ def _mangle(name: str, params: list[str]) -> str:
             out.append("i")
         elif t == "bool":
             out.append("b")
+        elif t == "double":
+            out.append("d")
         elif t == "constchar*":
             out.append("PKc")
         elif t == "double*":
@@ -51,14 +53,16 @@ def test_library_loads(built):
 def test_cpp_dropin_symbols(built):
     L = cs.lib()
     names = list(_decls(ROOT / "include" / "cuSten.h"))
-    assert len(names) == 50   # 12 x (create, swap, destroy, compute) + cuSenCompute2DXpFun + checkError
+    # 13 operators x (create, swap, destroy, compute) + cuSenCompute2DXpFun + checkError
+    assert len(names) == 54
     for name, params in names:
         mangled = _mangle(name, params)
         assert hasattr(L, mangled), f"missing {name} as {mangled}"
     # spot-check against names measured from the reference library build
     for m in ("_Z16cuStenCreate2DXpP8cuSten_tiiiiiiPdS1_S1_iii", "_Z17cuStenCompute2DXpP8cuSten_tb",
               "_Z14cuStenSwap2DXpP8cuSten_tPd", "_Z19cuSenCompute2DXpFunP8cuSten_tb",
-              "_Z17cuStenCreate2DXYpP8cuSten_tiiiiiiPdS1_S1_iiiiii"):
+              "_Z17cuStenCreate2DXYpP8cuSten_tiiiiiiPdS1_S1_iiiiii",
+              "_Z24cuStenCreate2DXYWENOADVpP8cuSten_tiiiiiiddPdS1_S1_S1_"):
         assert hasattr(L, m), m
 
 
