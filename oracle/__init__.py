@@ -27,7 +27,9 @@ SOURCES = [HERE / "stencil_oracle.c", HERE / "ch_oracle.c", HERE / "weno_oracle.
 HEADERS = [HERE / "stencil_oracle_impl.h"]
 
 REFRUN = BUILD / "librefrun.so"
+REFCH = BUILD / "librefch.so"
 REF_CUBIN = HERE / "_ref" / "custen_ref_sm103a.cubin"
+REF_CH_CUBIN = HERE / "_ref" / "custen_ref_ch_sm103a.cubin"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 
 _lib = None
@@ -49,6 +51,24 @@ def _build_refrun() -> None:
     os.replace(tmp, REFRUN)
 
 
+def _build_refch() -> None:
+    src = HERE / "ref_ch_runner.cpp"
+    if REFCH.exists() and REFCH.stat().st_mtime >= src.stat().st_mtime:
+        return
+    tmp = REFCH.with_suffix(".so.tmp")
+    libdirs = [CUDA_HOME / "lib64", CUDA_HOME / "lib64" / "stubs", CUDA_HOME / "targets" / "sbsa-linux" / "lib",
+               CUDA_HOME / "targets" / "sbsa-linux" / "lib" / "stubs"]
+    # contraction off: the program's host-side coefficients are plain IEEE expressions
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17", "-I", str(CUDA_HOME / "include"),
+           "-o", str(tmp), str(src)]
+    for d in libdirs:
+        if d.exists():
+            cmd += ["-L", str(d)]
+    cmd += ["-lcublas", "-lcudart", "-lcuda"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, REFCH)
+
+
 def build() -> Path:
     """Compile the C oracles (gcc, contraction off so that every fma is explicit)."""
     BUILD.mkdir(parents=True, exist_ok=True)
@@ -61,6 +81,7 @@ def build() -> Path:
         subprocess.run(cmd, check=True)
         os.replace(tmp, LIB)
     _build_refrun()
+    _build_refch()
     return LIB
 
 
@@ -241,3 +262,60 @@ def reference_weno(nx: int, ny: int, num_tiles: int, bx: int, by: int, out_ptr: 
     rc = Rr.refrun_weno(nx, ny, num_tiles, bx, by, out_ptr, in_ptr, u_ptr, v_ptr, float(cdx), float(cdy))
     if rc != 0:
         raise RuntimeError(Rr.refrun_error().decode())
+
+
+_refch = None
+
+
+class ReferenceCahnHilliardGPU:
+    """The reference's Cahn-Hilliard GPU program (cuPentCahnADITiming), device code unchanged, host loop
+    restated in oracle/ref_ch_runner.cpp: one grid, one step at a time with its device synchronisations.
+    Needs oracle/_ref/custen_ref_ch_sm103a.cubin (built where the reference sources exist)."""
+
+    @staticmethod
+    def available() -> bool:
+        return REF_CH_CUBIN.exists()
+
+    def __init__(self, c0: np.ndarray, lx: float = 2 * np.pi):
+        global _refch
+        if _refch is None:
+            build()
+            R = ctypes.CDLL(str(REFCH))
+            vp = ctypes.c_void_p
+            R.refch_error.restype = ctypes.c_char_p
+            R.refch_load.argtypes = [ctypes.c_char_p]
+            R.refch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_double, vp, vp, vp, vp]
+            R.refch_step.argtypes = [vp, ctypes.c_int]
+            R.refch_get.argtypes = [vp, vp, vp]
+            R.refch_destroy.argtypes = [vp]
+            if R.refch_load(str(REF_CH_CUBIN).encode()) != 0:
+                raise RuntimeError(R.refch_error().decode())
+            _refch = R
+        self._R = _refch
+        c0 = np.ascontiguousarray(c0, dtype=np.float64)
+        n = c0.shape[0]
+        self.n = n
+        tabs = CHOracle(c0, lx=lx).tables()
+        m = n - 2
+        inv1, inv2, omega = (np.ascontiguousarray(tabs[5 * m:6 * m]), np.ascontiguousarray(tabs[6 * m:7 * m]),
+                             np.ascontiguousarray(tabs[7 * m:7 * m + 4]))
+        h = ctypes.c_void_p()
+        if self._R.refch_create(ctypes.byref(h), n, float(lx), c0.ctypes.data, omega.ctypes.data, inv1.ctypes.data,
+                                inv2.ctypes.data) != 0:
+            raise RuntimeError(self._R.refch_error().decode())
+        self._h = h
+
+    def step(self, steps: int) -> None:
+        if self._R.refch_step(self._h, int(steps)) != 0:
+            raise RuntimeError(self._R.refch_error().decode())
+
+    def state(self):
+        cur, old = np.empty((self.n, self.n)), np.empty((self.n, self.n))
+        if self._R.refch_get(self._h, cur.ctypes.data, old.ctypes.data) != 0:
+            raise RuntimeError(self._R.refch_error().decode())
+        return cur, old
+
+    def close(self) -> None:
+        if self._h:
+            self._R.refch_destroy(self._h)
+            self._h = None

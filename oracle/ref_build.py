@@ -6,8 +6,11 @@ oracle/_ref (git-ignored). Where the sources are absent (e.g. on the GPU machine
 and the prebuilt outputs are used if they are present.
 
 Outputs:
-  custen_ref_sm103a.cubin -- the twelve cuSten kernels, unchanged, for sm_103a (oracle/ref_kernels.cu),
-                             driven by oracle/ref_runner.cpp. CUDA 13 removed one cudaMemPrefetchAsync
+  custen_ref_sm103a.cubin -- the thirteen cuSten kernels, unchanged, for sm_103a (oracle/ref_kernels.cu),
+                             driven by oracle/ref_runner.cpp.
+  custen_ref_ch_sm103a.cubin -- the device code of cuPentSpeedUp/cuPentCahnADITiming (its element-wise
+                             kernels, nonLinRHS, the batched pentadiagonal solves and the two cuSten XY
+                             kernels it uses), driven by oracle/ref_ch_runner.cpp. CUDA 13 removed one cudaMemPrefetchAsync
                              overload the reference calls; oracle/ref_compat.h restores it.
   libserialch.so          -- cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c compiled with gcc as the
                              reference's compile.sh does (-O3, no contraction flags), its main renamed,
@@ -26,6 +29,7 @@ ROOT = HERE.parent
 REF = Path(os.environ.get("CUSTEN_REFERENCE_ROOT", "/root/reference"))
 OUT = HERE / "_ref"
 CUBIN = OUT / "custen_ref_sm103a.cubin"
+CH_CUBIN = OUT / "custen_ref_ch_sm103a.cubin"
 SERIAL_SO = OUT / "libserialch.so"
 
 
@@ -48,6 +52,21 @@ def build_cubin() -> Path:
     return CUBIN
 
 
+def build_ch_cubin() -> Path:
+    """The device code of the reference's Cahn-Hilliard GPU timing program (oracle/ref_ch_kernels.cu)."""
+    OUT.mkdir(parents=True, exist_ok=True)
+    stub = OUT / "hdf5_stub"
+    stub.mkdir(exist_ok=True)
+    (stub / "hdf5.h").write_text("/* empty: the reference program includes hdf5.h; its device code uses nothing from it */\n")
+    tmp = CH_CUBIN.with_suffix(".cubin.tmp")
+    cmd = [_nvcc(), "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++14",
+           "-include", str(HERE / "ref_compat.h"), "-I", str(ROOT), "-I", str(stub), f"-DREF_ROOT={REF}",
+           "-o", str(tmp), str(HERE / "ref_ch_kernels.cu")]
+    subprocess.run(cmd, check=True, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    os.replace(tmp, CH_CUBIN)
+    return CH_CUBIN
+
+
 def build_serial_ch() -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
     stub = OUT / "hdf5_stub"
@@ -66,6 +85,7 @@ def build_if_available() -> None:
     if not available():
         return
     build_cubin()
+    build_ch_cubin()
     if (HERE / "ref_serial_ch.c").exists():
         build_serial_ch()
 
