@@ -187,6 +187,121 @@ def cpu_sample(n: int, rows: int, threads: int):
     return one_pass
 
 
+def cpu_ch_sample(steps: int = 40, n: int = 256) -> dict:
+    """The serial Cahn-Hilliard solver (oracle port of cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c,
+    single-threaded as the reference program is) on config 1's grid: 256^2, lx = 2 pi, bounded steps."""
+    import numpy as np
+
+    import oracle
+    c0 = np.random.default_rng(0).uniform(-0.1, 0.1, (n, n))
+    o = oracle.CHOracle(c0)
+    o.step(2)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    return {"value": round(steps / dt, 2), "unit": "steps/s", "gpt_steps_per_s": round(n * n * steps / dt / 1e9, 5),
+            "cores": 1, "kind": "port", "sample": f"{n}^2 grid, {steps} steps (serial ADI solver, one thread)"}
+
+
+def reference_gpu(args) -> dict:
+    """The reference's own device code rebuilt for sm_103a on this GPU (cubins compiled unchanged from the
+    reference sources; host loops restated in oracle/ref_runner.cpp and oracle/ref_ch_runner.cpp)."""
+    try:
+        import numpy as np
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU visible"}
+        import oracle
+        if oracle.reference_kernels() is None:
+            return {"unavailable": "reference cubins not built (they are compiled from the reference sources)"}
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    dev = torch.device("cuda", 0)
+    n = args.n
+    out = {}
+    x = torch.arange(n, device=dev, dtype=torch.float64) * (2 * math.pi / n)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    f = (torch.sin(3 * x)[None, :] * torch.cos(5 * x)[:, None] +
+         (torch.rand((n, n), device=dev, dtype=torch.float64, generator=g) * 2e-3 - 1e-3)).contiguous()
+    o = torch.zeros_like(f)
+    per, total = {}, 0.0
+    for (nm, v, H, L, R, V, T, B, w, fun, _) in operators(n):
+        wt = torch.tensor(w, dtype=torch.float64, device=dev)
+        d = 0 if v < 4 else (1 if v < 8 else 2)
+        num_sten = H * V if d == 2 else (H if d == 0 else V)
+        func = oracle.reference_fun_ptr(fun) if fun >= 0 else 0
+
+        def call():
+            oracle.reference_compute(v, n, n, 1, 32, 8, o.data_ptr(), f.data_ptr(), wt.data_ptr(), num_sten=num_sten,
+                                     H=H, L=L, R=R, V=V, T=T, B=B, num_coe=len(w), func=func)
+        call()
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            call()
+        dt = (time.perf_counter() - t0) / reps
+        total += dt
+        per[nm] = round(n * n / dt / 1e9, 3)
+    out["stencil_sweep"] = {"gpts_s": round(12 * n * n / total / 1e9, 3), "unit": "Gpts/s", "per_op": per,
+                            "config": f"{n}^2, the 12 operators of the headline sweep, BLOCK 32x8, numTiles 1",
+                            "method": "reference kernels, one launch per Compute, wall time of each synchronised "
+                                      "Compute (XpFun with the shared-memory layout its kernel indexes)"}
+    # WENO advection
+    rng = np.random.default_rng(1)
+    u = torch.tensor(rng.uniform(-1, 1, (n, n)), device=dev)
+    vv = torch.tensor(rng.uniform(-1, 1, (n, n)), device=dev)
+    h = 2 * math.pi / n
+    oracle.reference_weno(n, n, 1, 32, 8, o.data_ptr(), f.data_ptr(), u.data_ptr(), vv.data_ptr(), 1 / h, 1 / h)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        oracle.reference_weno(n, n, 1, 32, 8, o.data_ptr(), f.data_ptr(), u.data_ptr(), vv.data_ptr(), 1 / h, 1 / h)
+    dt = (time.perf_counter() - t0) / 3
+    out["weno"] = {"gpts_s": round(n * n / dt / 1e9, 3), "config": f"{n}^2, BLOCK 32x8, u, v ~ U(-1, 1)"}
+    del f, o, u, vv
+    torch.cuda.empty_cache()
+    # Cahn-Hilliard: the reference program, one grid at a time
+    if oracle.ReferenceCahnHilliardGPU.available():
+        step_s = {}
+        for m in (64, 128, 256, 512, 1024, 2048):
+            c0 = np.random.default_rng(m).uniform(-0.1, 0.1, (m, m))
+            r = oracle.ReferenceCahnHilliardGPU(c0)
+            r.step(2)
+            k = 20 if m <= 1024 else 8
+            t0 = time.perf_counter()
+            r.step(k)
+            step_s[m] = (time.perf_counter() - t0) / k
+            r.close()
+        sizes = [int(v) for v in np.random.default_rng(2).choice([64, 128, 256, 512, 1024], size=args.ch_sims)]
+        total_b = sum(step_s[m] * args.ch_steps for m in sizes)
+        served = served_workload(args)
+        ms = sorted(step_s)
+
+        def t_of(m):   # piecewise linear in m^2 between the measured sizes (multiples of 64)
+            for lo, hi in zip(ms, ms[1:]):
+                if m <= hi:
+                    a = (m * m - lo * lo) / (hi * hi - lo * lo)
+                    return step_s[lo] + a * (step_s[hi] - step_s[lo])
+            return step_s[ms[-1]]
+        t, ttc = 0.0, []
+        for arr, m, k in zip(*served):
+            start = max(t, arr)
+            t = start + k * t_of(m)
+            ttc.append(t - arr)
+        out["ch_plain_loop"] = {
+            "step_ms_by_n": {str(m): round(v * 1e3, 4) for m, v in step_s.items()},
+            "batched_config_steps_per_s": round(len(sizes) * args.ch_steps / total_b, 1),
+            "served_config": {"makespan_s": round(t, 3), "steps_per_s": round(sum(served[2]) / t, 1),
+                              "ttc_p50_s": round(float(np.percentile(ttc, 50)), 3),
+                              "ttc_p99_s": round(float(np.percentile(ttc, 99)), 3)},
+            "method": "cuPentCahnADITiming device code unchanged, its host loop restated (device synchronisation "
+                      "after every kernel); per-size step time x steps summed over the batch; served: FCFS over "
+                      "the request stream with step times interpolated in n^2 between measured sizes"}
+    else:
+        out["ch_plain_loop"] = {"unavailable": "reference CH cubin not built"}
+    return out
+
+
 def run_reference_arm(args, world, rank):
     if rank != 0:
         return
@@ -210,7 +325,10 @@ def run_reference_arm(args, world, rank):
         "cpu_baseline": {"value": round(v, 4), "unit": "Gpts/s", "cores": threads, "kind": "port",
                          "sample": f"{rows} rows x {args.n} columns per operator, 12 operators, plain host loop"},
         "e2e": {"value": round(v, 4), "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_ch": cpu_ch_sample(),
     }
+    if not args.skip_ref_gpu:
+        line["gpu_sm103a"] = reference_gpu(args)
     print(json.dumps(line), flush=True)
 
 
@@ -332,6 +450,16 @@ def run_gpu(args, world, rank, local):
         del inp32, outs32, hs32, keep32
         torch.cuda.synchronize(dev)
 
+    # ---- config 2 across sizes: n = 1024 .. 8192, numTiles 1 and 4 (16384 is the headline above) ----
+    sizes_out = None
+    if not args.skip_sizes:
+        sizes_out = run_size_sweep(cs, torch, dev, local)
+
+    # ---- WENO5 advection (the thirteenth operator), FP64 ----
+    weno = None
+    if not args.skip_weno:
+        weno = run_weno(cs, torch, dev, n, fp64_rate)
+
     # ---- e2e: reference-facing API with host buffers (numTiles=4, HOST offload) ----
     e2e = e2e_managed = None
     if not args.skip_e2e:
@@ -358,10 +486,21 @@ def run_gpu(args, world, rank, local):
     torch.cuda.synchronize(dev)
     torch.cuda.empty_cache()
 
-    ch_batched = ch_served = None
+    ch_batched = ch_served = cpu_ch = None
     if not args.skip_ch:
         ch_batched = run_ch_batched(args, cs)
         ch_served = None if args.skip_served else run_ch_served(args, cs)
+        pts_b = ch_batched["points"] * args.ch_steps
+        ch_batched["roofline"] = {
+            "bound": "fp64", "algorithmic_bytes_per_point_step": 56,
+            "achieved_gbs": round(56.0 * ch_batched["fp64"]["gpt_steps_per_s"], 1), "hbm_peak_gbs": hbm_peak,
+            "hbm_frac": round(56.0 * ch_batched["fp64"]["gpt_steps_per_s"] / hbm_peak, 4),
+            "fp64_ops_per_point_step": 40,
+            "fp64_frac": round(40e9 * ch_batched["fp64"]["gpt_steps_per_s"] / fp64_rate, 3),
+            "note": "FP64-pipe bound: about 40 FP64 operations per point and step against 56 compulsory bytes"}
+        del pts_b
+        if rank == 0 and not args.skip_cpu:
+            cpu_ch = cpu_ch_sample()
 
     if rank == 0:
         line = {
@@ -392,6 +531,12 @@ def run_gpu(args, world, rank, local):
             line["e2e_managed"] = e2e_managed
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if sizes_out is not None:
+            line["sizes"] = sizes_out
+        if weno is not None:
+            line["weno"] = weno
+        if cpu_ch is not None:
+            line["cpu_baseline_ch"] = cpu_ch
         if ch_batched is not None:
             line["ch_batched"] = ch_batched
             if ch_served is not None:
@@ -468,6 +613,99 @@ def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
 
 
 # ----------------------------------------------------------------------------------------------
+# Stencil sweep across sizes (config 2) and the WENO operator
+# ----------------------------------------------------------------------------------------------
+def run_size_sweep(cs, torch, dev, local, sizes=(1024, 2048, 4096, 8192), tiles=(1, 4)):
+    """The 12-operator FP64 sweep at smaller grids, device-resident, numTiles 1 and 4. For n <= 2048 the
+    sweep is captured once in a CUDA graph and the graph is replayed (launch latency would dominate);
+    otherwise sweeps are timed with events. Median of the timed repetitions."""
+    out = {}
+    for n in sizes:
+        ops = operators(n)
+        x = torch.arange(n, device=dev, dtype=torch.float64) * (2 * math.pi / n)
+        inp = (torch.sin(3 * x)[None, :] * torch.cos(5 * x)[:, None]).contiguous()
+        for nt in tiles:
+            outs, hs, keep = [], [], []
+            for (nm, v, H, L, R, V, T, B, w, fun, _) in ops:
+                wt = torch.tensor(w, device=dev, dtype=torch.float64)
+                o = torch.zeros((n, n), device=dev, dtype=torch.float64)
+                func = cs.builtin_function(fun, cs.F64) if fun >= 0 else None
+                hs.append(cs.Stencil(v, n, n, o, inp, wt, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=nt, block_x=32,
+                                     block_y=8, dtype=cs.F64, device=local, ncoef=len(w), func=func))
+                outs.append(o)
+                keep.append(wt)
+            side = torch.cuda.Stream(dev)
+            with torch.cuda.stream(side):
+                for h in hs:
+                    h.compute(stream=side)
+            torch.cuda.synchronize(dev)
+            graph = None
+            if n <= 2048:
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph, capture_error_mode="relaxed"):
+                    cap = torch.cuda.current_stream(dev)
+                    for h in hs:
+                        h.compute(stream=cap)
+                graph.replay()
+                torch.cuda.synchronize(dev)
+            reps, times = 20, []
+            s = torch.cuda.current_stream(dev)
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                if graph is not None:
+                    graph.replay()
+                else:
+                    for h in hs:
+                        h.compute(stream=s)
+                e1.record(s)
+                torch.cuda.synchronize(dev)
+                times.append(e0.elapsed_time(e1))
+            ms = sorted(times)[len(times) // 2]
+            out[f"{n}_tiles{nt}"] = {"gpts_s": round(len(ops) * n * n / (ms * 1e-3) / 1e9, 3),
+                                     "ms_per_sweep": round(ms, 4), "timing": "graph replay" if graph else "events"}
+            for h in hs:
+                h.destroy()
+            del graph, outs, keep
+        del inp
+        torch.cuda.synchronize(dev)
+    return out
+
+
+def run_weno(cs, torch, dev, n, fp64_rate):
+    """cuStenCompute2DXYWENOADVp at n^2: out = u * WENO5_x + v * WENO5_y, u, v ~ U(-1, 1), 32 B/pt."""
+    import numpy as np
+    rng = np.random.default_rng(1)
+    x = torch.arange(n, device=dev, dtype=torch.float64) * (2 * math.pi / n)
+    f = (torch.sin(3 * x)[None, :] * torch.cos(5 * x)[:, None]).contiguous()
+    u = torch.tensor(rng.uniform(-1, 1, (n, n)), device=dev)
+    v = torch.tensor(rng.uniform(-1, 1, (n, n)), device=dev)
+    o = torch.zeros_like(f)
+    h = 2 * math.pi / n
+    op = cs.WenoAdvection(n, n, o, f, u, v, dx=h, dy=h, block_x=32, block_y=8)
+    s = torch.cuda.current_stream(dev)
+    op.compute(stream=s)
+    torch.cuda.synchronize(dev)
+    times = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        op.compute(stream=s)
+        e1.record(s)
+        torch.cuda.synchronize(dev)
+        times.append(e0.elapsed_time(e1))
+    op.destroy()
+    ms = sorted(times)[len(times) // 2]
+    gpts = n * n / (ms * 1e-3) / 1e9
+    del f, u, v, o
+    torch.cuda.empty_cache()
+    return {"gpts_s": round(gpts, 3), "ms": round(ms, 3), "hbm_gbs": round(32.0 * gpts, 1),
+            "config": f"{n}^2, periodic, u, v ~ U(-1, 1), dx = dy = 2 pi / n",
+            "note": "FP64-pipe bound: about 200 FP64 operations per point (eight correctly rounded divisions) "
+                    "against 32 bytes"}
+
+
+# ----------------------------------------------------------------------------------------------
 # Cahn-Hilliard ADI: batched (config 4) and served (config 5)
 # ----------------------------------------------------------------------------------------------
 def plain_step_seconds(cs, n: int, steps: int = 10) -> float:
@@ -524,17 +762,26 @@ def run_ch_batched(args, cs):
     return out
 
 
-def run_ch_served(args, cs):
-    """Poisson arrivals (mean rate, seed 3), N log-uniform 128-2048 rounded to 32, steps U(100, 5000),
-    c0 ~ U(-0.1, 0.1), HBM budget 150 GB, a fixed number of requests."""
+def served_workload(args):
+    """(arrival times, grid sizes, step counts) of the served request stream: Poisson arrivals (mean rate,
+    seed 3), N log-uniform 128-2048 rounded to a multiple of 32, steps U(100, 5000)."""
     import numpy as np
     rng = np.random.default_rng(3)
     R = args.served_requests
     gaps = rng.exponential(1.0 / args.served_rate, size=R)
-    arrivals = np.cumsum(gaps) - gaps[0]
+    arrivals = [float(a) for a in np.cumsum(gaps) - gaps[0]]
     sizes = [int(max(128, min(2048, round(math.exp(v) / 32) * 32)))
              for v in rng.uniform(math.log(128), math.log(2048), size=R)]
     steps = [int(v) for v in rng.integers(100, 5001, size=R)]
+    return arrivals, sizes, steps
+
+
+def run_ch_served(args, cs):
+    """Poisson arrivals (mean rate, seed 3), N log-uniform 128-2048 rounded to 32, steps U(100, 5000),
+    c0 ~ U(-0.1, 0.1), HBM budget 150 GB, a fixed number of requests."""
+    import numpy as np
+    R = args.served_requests
+    arrivals, sizes, steps = served_workload(args)
     srv = cs.CahnHilliardServer(hbm_budget_bytes=150e9, chunk_steps=args.served_chunk, keep_results=False)
     for k in range(R):
         srv.submit(sizes[k], steps[k], arrival=float(arrivals[k]), seed=1000 + k)
@@ -588,6 +835,9 @@ def main():
     ap.add_argument("--served-requests", type=int, default=48)
     ap.add_argument("--served-rate", type=float, default=200.0)
     ap.add_argument("--served-chunk", type=int, default=16)
+    ap.add_argument("--skip-ref-gpu", action="store_true")
+    ap.add_argument("--skip-sizes", action="store_true")
+    ap.add_argument("--skip-weno", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch from an ncu capture (recorded in the roofline object)")
     args = ap.parse_args()
