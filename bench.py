@@ -43,21 +43,21 @@ def operators(n: int):
     w5 = [w / (12 * h * h) for w in W5]
     wc = [w / (4 * h * h) for w in WCROSS]
     wl = [w / (h * h) for w in WLAP]
-    # FP64 operations per point: weights skip exact zeros; Fun variants apply c^3-c (mul + fma) per
-    # window point and an fma per coefficient (zeros included: the user function decides).
+    # FP64 operations per point: weights skip exact zeros; the Fun variants run the library's c^3 - c
+    # functions fused: c^3 - c (mul + fma) once per input value, then an fma per non-zero coefficient.
     ops = []
     for nm, v in (("Xp", 0), ("Xnp", 1)):
         ops.append((nm, v, 5, 2, 2, 1, 0, 0, w5, -1, 5))
     for nm, v in (("XpFun", 2), ("XnpFun", 3)):
-        ops.append((nm, v, 5, 2, 2, 1, 0, 0, w5, 1, 15))
+        ops.append((nm, v, 5, 2, 2, 1, 0, 0, w5, 1, 7))
     for nm, v in (("Yp", 4), ("Ynp", 5)):
         ops.append((nm, v, 1, 0, 0, 5, 2, 2, w5, -1, 5))
     for nm, v in (("YpFun", 6), ("YnpFun", 7)):
-        ops.append((nm, v, 1, 0, 0, 5, 2, 2, w5, 3, 15))
+        ops.append((nm, v, 1, 0, 0, 5, 2, 2, w5, 3, 7))
     for nm, v in (("XYp", 8), ("XYnp", 9)):
         ops.append((nm, v, 3, 1, 1, 3, 1, 1, wc, -1, 4))
     for nm, v in (("XYpFun", 10), ("XYnpFun", 11)):
-        ops.append((nm, v, 3, 1, 1, 3, 1, 1, wl, 5, 27))
+        ops.append((nm, v, 3, 1, 1, 3, 1, 1, wl, 5, 7))
     return ops
 
 
@@ -432,6 +432,25 @@ def run_gpu(args, world, rank, local):
                    "hbm_gbs": round(16.0 * n * n / (ms * 1e-3) / 1e9, 1),
                    "fp64_frac": round(dfma_pt * n * n / (ms * 1e-3) / fp64_rate, 3)}
 
+    # ---- the six Fun operators again with the indirect call (library function fusion off) ----
+    fun_indirect = None
+    if not args.skip_indirect:
+        fun_hs = [(nm, h) for (nm, *_r), h in zip(ops, hs64) if nm.endswith("Fun")]
+        cs.set_fun_fusion(False)
+        try:
+            _, per_ind, _ = timed_sweep([h for _, h in fun_hs], max(1, args.steps), 1)
+        finally:
+            cs.set_fun_fusion(True)
+        fun_indirect = {"per_op": {nm: {"gpts_s": round(n * n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 4)}
+                                   for (nm, _), ms in zip(fun_hs, per_ind)},
+                        "sweep_gpts_s_with_indirect_fun": round(
+                            pts_step / ((kernel_ms - sum(per[nm]["ms"] for nm, _ in fun_hs) + sum(per_ind)) * 1e-3)
+                            / 1e9, 3),
+                        "note": "the Fun operators use the library's c^3 - c device functions; the headline runs "
+                                "them fused (one cube per input value, then the coefficients as weights, "
+                                "bit-identical); here each output point calls the function through its "
+                                "pointer, as a user-defined function does"}
+
     # ---- FP32 precision variant: same sweep in FP32, error against the FP64 outputs ----
     fp32 = None
     if not args.skip_fp32:
@@ -531,6 +550,8 @@ def run_gpu(args, world, rank, local):
             line["e2e_managed"] = e2e_managed
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if fun_indirect is not None:
+            line["fun_indirect"] = fun_indirect
         if sizes_out is not None:
             line["sizes"] = sizes_out
         if weno is not None:
@@ -838,6 +859,7 @@ def main():
     ap.add_argument("--skip-ref-gpu", action="store_true")
     ap.add_argument("--skip-sizes", action="store_true")
     ap.add_argument("--skip-weno", action="store_true")
+    ap.add_argument("--skip-indirect", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch from an ncu capture (recorded in the roofline object)")
     args = ap.parse_args()

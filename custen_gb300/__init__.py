@@ -55,6 +55,9 @@ def lib() -> ctypes.CDLL:
         L.custen_transfer_bytes.restype = None
         L.custen_set_stage_chunk_bytes.argtypes = [sz]
         L.custen_set_stage_chunk_bytes.restype = None
+        L.custen_set_fun_fusion.argtypes = [i]
+        L.custen_set_fun_fusion.restype = None
+        L.custen_builtin_fun_id.argtypes = [vp, i]
         L.custen_device_error.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
         L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
         L.custen_create_2d_xyweno_adv_p.argtypes = [vp, i, i, i, i, i, i, ctypes.c_double, ctypes.c_double, vp, vp,
@@ -147,6 +150,11 @@ def transfer_bytes() -> tuple:
     h2d, d2h = ctypes.c_ulonglong(), ctypes.c_ulonglong()
     lib().custen_transfer_bytes(ctypes.byref(h2d), ctypes.byref(d2h))
     return int(h2d.value), int(d2h.value)
+
+
+def set_fun_fusion(enable: bool) -> None:
+    """Fused path for the library's own c^3 - c Fun functions (default on); off = indirect calls."""
+    lib().custen_set_fun_fusion(int(bool(enable)))
 
 
 def set_stage_chunk_bytes(nbytes: int) -> None:

@@ -68,3 +68,22 @@ extern "C" int custen_builtin_function(int id, int dtype, void** func) {
     *func = p;
     return 0;
 }
+
+// Which shipped function `f` is on the current device (0..5), or -1. The twelve addresses are read once
+// per device.
+extern "C" int custen_builtin_fun_id(const void* f, int dtype) {
+    static void* cache[64][2][6];
+    static bool ready[64] = {};
+    int dev = 0;
+    if (f == nullptr || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    if (!ready[dev]) {
+        for (int t = 0; t < 2; ++t)
+            for (int id = 0; id < 6; ++id)
+                if (custen_builtin_function(id, t == 0 ? CUSTEN_F64 : CUSTEN_F32, &cache[dev][t][id]) != 0) return -1;
+        ready[dev] = true;
+    }
+    const int t = dtype == CUSTEN_F64 ? 0 : 1;
+    for (int id = 0; id < 6; ++id)
+        if (cache[dev][t][id] == f) return id;
+    return -1;
+}

@@ -51,6 +51,10 @@ struct StencilArgs {
     int wrap_x;           // 1: columns outside [0,nx) wrap around (periodic variants)
     int has_top, has_bot; // 1: halo rows above / below may be read
     int vec_ok;           // 1: rows are 16-byte aligned, vector loads/stores allowed
+    // 1: every staged input value c is replaced by c^3 - c (as fma(c*c, c, -c)) and the coefficients then
+    // apply as plain weights. Set for the Fun variants when the device function is one of the library's
+    // own c^3 - c functions, which compute exactly that (builtin_funs.cuh, ids 1, 3, 5).
+    int pre;
     // WENO advection only: velocity rows row0.. and the inverse grid spacings (coeDx, coeDy)
     const void* u;
     const void* v;
@@ -122,6 +126,10 @@ struct PlanPrivate {
     cudaStream_t user_stream;
     int use_user_stream;
     unsigned long long launches;   // kernels launched by this handle (for instrumentation)
+    // Fun variants: the device function last checked against the library's own functions, and whether
+    // it can run as c^3 - c followed by plain weights (StencilArgs::pre).
+    void* fused_func;
+    int fused_pre;
     // Host-resident fields (pinned or system memory) are streamed through device staging slots:
     // kStageSlots slots of (T + chunk + B) input rows and chunk output rows, plus the weights.
     // Allocated at the first such Compute, freed by Destroy.

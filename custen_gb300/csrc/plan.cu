@@ -26,6 +26,10 @@ static_assert(offsetof(cuSten_t, weights) == 104, "cuSten_t::weights offset");
 static_assert(offsetof(cuSten_t, streams) == 176, "cuSten_t::streams offset");
 static_assert(offsetof(cuSten_t, devFunc) == 192, "cuSten_t::devFunc offset");
 
+// The shipped Fun functions live in the shared library (builtin_funs.cu); a program linking only the
+// static archive has none, and every device function takes the indirect-call path.
+extern "C" int custen_builtin_fun_id(const void* f, int dtype) __attribute__((weak));
+
 namespace custen {
 
 // Device-side error word: bit 0 = an mbarrier wait of a TMA-staged kernel expired.
@@ -37,6 +41,7 @@ static std::atomic<unsigned long long> g_launches_tma{0};
 static std::atomic<unsigned long long> g_h2d_bytes{0};   // host -> device bytes moved by Compute
 static std::atomic<unsigned long long> g_d2h_bytes{0};   // device -> host bytes moved by Compute
 static std::atomic<size_t> g_stage_chunk_bytes{(size_t)32 << 20};   // staging chunk size, host-resident fields
+static std::atomic<int> g_fun_fusion{1};   // run the library's own c^3 - c Fun functions as cube + weights
 
 enum { ST_OK = 0, ST_CUDA = 1, ST_ARG = 2, ST_UNSUPPORTED = 3 };
 
@@ -163,6 +168,8 @@ int create_plan(cuSten_t* h, int variant, int dtype, int dev, int numTiles, int 
     p.user_stream = nullptr;
     p.use_user_stream = 0;
     p.launches = 0;
+    p.fused_func = nullptr;
+    p.fused_pre = 0;
     p.stage = nullptr;
     p.stage_slot_bytes = 0;
     p.stage_rows = 0;
@@ -541,6 +548,18 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
     a.nyTile = nyT;
     a.numTiles = nt;
     a.wrap_x = periodic && dir != 1;
+    if (variant_is_fun(p->variant) && g_fun_fusion.load(std::memory_order_relaxed)) {
+        // The library's own c^3 - c functions (ids 1, 3, 5) with the window they read: cube each staged
+        // value once, then apply the coefficients as plain weights (bit-identical, fewer FP64 operations).
+        if (h->devFunc != p->fused_func) {
+            p->fused_func = h->devFunc;
+            const int id = custen_builtin_fun_id ? custen_builtin_fun_id(h->devFunc, p->dtype) : -1;
+            p->fused_pre = (id == 1 && dir == 0 && p->L == 2 && p->R == 2 && p->ncoef == 5) ||
+                           (id == 3 && dir == 1 && p->T == 2 && p->B == 2 && p->ncoef == 5) ||
+                           (id == 5 && dir == 2 && p->ncoef == p->H * p->V);
+        }
+        a.pre = p->fused_pre;
+    }
     if (p->variant == V_XYWENOADVP) {
         // the reference passes coeDx / coeDy from the handle at every Compute (2d_xyADVWENO_p_kernel.cu:479-480)
         a.cdx = h->coeDx;
@@ -785,6 +804,7 @@ int custen_sizeof_handle(void) { return (int)sizeof(cuSten_t); }
 const char* custen_last_error(void) { return g_last_error.c_str(); }
 unsigned long long custen_kernel_launches(void) { return g_launches.load(); }
 unsigned long long custen_kernel_launches_tma(void) { return g_launches_tma.load(); }
+void custen_set_fun_fusion(int enable) { g_fun_fusion.store(enable ? 1 : 0); }
 void custen_set_stage_chunk_bytes(size_t bytes) { g_stage_chunk_bytes.store(bytes ? bytes : (size_t)32 << 20); }
 void custen_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h) {
     if (h2d) *h2d = g_h2d_bytes.load();

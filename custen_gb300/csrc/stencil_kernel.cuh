@@ -14,6 +14,7 @@
 // the geometry allows; this file holds the compute/store stage and the plain-load staging path.
 #pragma once
 
+#include "builtin_funs.cuh"
 #include "custen_internal.h"
 
 namespace custen {
@@ -86,6 +87,14 @@ __device__ __forceinline__ int stage_coefficients(const StencilArgs& a, T* coef_
     }
     __syncthreads();
     return is_fun ? 0 : s_count;
+}
+
+// c -> c^3 - c over a staged window, once per staged value (StencilArgs::pre): the operation of the
+// library's c^3 - c Fun functions (builtin_funs.cuh, cube_minus), so that the weights applied afterwards
+// give their results bit for bit with one cube per input value instead of one per window point.
+template <typename T, int NT>
+__device__ __forceinline__ void apply_cube(T* tile, int count, int tid) {
+    for (int e = tid; e < count; e += NT) tile[e] = custen_funs::cube_minus<T>(tile[e]);
 }
 
 // Plain-load staging of the window (16-byte vector loads where the whole vector is in range).

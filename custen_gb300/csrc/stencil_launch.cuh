@@ -25,10 +25,14 @@ stencil_ldg_kernel(const __grid_constant__ StencilArgs a) {
     int* list_off = reinterpret_cast<int*>(smem + g.list_off(a));
     T* list_w = reinterpret_cast<T*>(smem + g.listw_off(a));
     const int tid = threadIdx.x + threadIdx.y * NTX;
-    const bool is_fun = variant_is_fun(a.variant);
+    const bool is_fun = variant_is_fun(a.variant) && !a.pre;
     const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
     stage_tile_ldg<T, TW, TH, NT>(a, tile, g, x0, y0, tid);
     const int nlist = stage_coefficients<T, NT>(a, coef_s, list_off, list_w, g.SW, tid, is_fun);  // syncs
+    if (a.pre) {
+        apply_cube<T, NT>(tile, g.SR * g.SW, tid);
+        __syncthreads();
+    }
     const bool all_write = tile_all_write(a, x0, x0 + TW, a.row0 + y0, a.row0 + y0 + TH);
     compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
                                       threadIdx.y, is_fun, all_write);
@@ -141,7 +145,7 @@ cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
 
 template <typename T, int TW, int TH, int RPT, int S>
 cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
-    const int mode = variant_is_fun(a.variant) ? (int)MODE_FUN : shape_mode(a.H, a.L, a.V, a.T);
+    const int mode = (variant_is_fun(a.variant) && !a.pre) ? (int)MODE_FUN : shape_mode(a.H, a.L, a.V, a.T);
     switch (mode) {
     case MODE_FUN: return launch_tma_mode<T, TW, TH, RPT, S, MODE_FUN>(a, s);
     case 2: return launch_tma_mode<T, TW, TH, RPT, S, 2>(a, s);

@@ -192,6 +192,10 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
             edge_fixup<T, TW, TH, NT>(a, tile, g, x0, y0, tid, rows_fix, cols_fix);
             __syncthreads();
         }
+        if (a.pre) {
+            apply_cube<T, NT>(tile, (int)stage_elems, tid);
+            __syncthreads();
+        }
         const bool all_write = tile_all_write(a, x0, x0 + TW, a.row0 + y0, a.row0 + y0 + TH);
         if constexpr (MODE >= MODE_FIRST_SHAPE) {
             using SH = typename ShapeOf<MODE>::type;

@@ -44,6 +44,13 @@ void custen_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h);
 /* Fields in pinned or system memory are streamed through device staging slots in chunks of about
  * `bytes` (0: the default, 32 MiB); applies to handles whose first such Compute comes later. */
 void custen_set_stage_chunk_bytes(size_t bytes);
+/* Fun variants whose device function is one of the library's c^3 - c functions (custen_builtin_function
+ * ids 1, 3, 5, with the window that function reads) run as c^3 - c once per input value followed by the
+ * coefficients as plain weights: bit-identical results, fewer FP64 operations. enable = 0 sends them
+ * through the indirect call like any user function. Default 1. No reference counterpart. */
+void custen_set_fun_fusion(int enable);
+/* Which shipped function (0..5) `f` is on the current device, or -1. */
+int custen_builtin_fun_id(const void* f, int dtype);
 
 /* ---- handle life cycle: generic form ----
  * H/L/R: window width and extents in x; V/T/B in y. X variants: V=1, T=B=0; Y variants: H=1, L=R=0.

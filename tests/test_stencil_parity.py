@@ -133,6 +133,27 @@ def test_parity_reference_example_functions(gpu, variant):
     check(got, ref, st, pre)
 
 
+@pytest.mark.parametrize("variant", [cs.XPFUN, cs.XNPFUN, cs.YPFUN, cs.YNPFUN, cs.XYPFUN, cs.XYNPFUN])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_fused_and_indirect_fun_paths_agree(gpu, variant, dtype):
+    """The library's c^3 - c functions run fused (cube once per value, then weights) by default and through
+    the indirect call when fusion is off: both give the oracle's result and are bitwise identical."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    geom = {0: (5, 2, 2, 1, 0, 0), 1: (1, 0, 0, 5, 2, 2), 2: (3, 1, 1, 3, 1, 1)}[d]
+    nx, ny = (128, 64) if d != 1 else (64, 128)
+    got_fused, ref, st, pre = run_both(variant, nx, ny, 2, 32 if d != 1 else 16, 8, geom, dtype=dtype,
+                                       fun_id=FUN_IDS[d][1], seed=17 + variant)
+    check(got_fused, ref, st, pre)
+    cs.set_fun_fusion(False)
+    try:
+        got_call, *_ = run_both(variant, nx, ny, 2, 32 if d != 1 else 16, 8, geom, dtype=dtype,
+                                fun_id=FUN_IDS[d][1], seed=17 + variant)
+    finally:
+        cs.set_fun_fusion(True)
+    check(got_call, ref, st, pre)
+    assert got_fused.tobytes() == got_call.tobytes()
+
+
 @pytest.mark.parametrize("variant", [cs.XP, cs.YNP, cs.XYP, cs.XYNPFUN])
 def test_managed_memory_tile_streaming(gpu, variant):
     """Managed memory, numTiles = 4, HOST offload: tiles stream through the GPU and come back."""
