@@ -32,6 +32,10 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+# ncu DRAM bytes (read + write) per stencil launch, mean over the 12 operators of the sweep at 6144^2
+# (profiles/stencil_sweep_traffic.md); the field is streamed once per launch, so it scales with n^2.
+TRAFFIC_6144 = 559918997.0
+
 W5 = [-1.0, 16.0, -30.0, 16.0, -1.0]
 WCROSS = [1.0, 0.0, -1.0, 0.0, 0.0, 0.0, -1.0, 0.0, 1.0]
 WLAP = [0.0, 1.0, 0.0, 1.0, -4.0, 1.0, 0.0, 1.0, 0.0]
@@ -532,7 +536,10 @@ def run_gpu(args, world, rank, local):
                        "nx": n, "ny": n, "numTiles": 1, "l2": "inputs larger than L2 (2 GiB per field)",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
-                         "frac": round(achieved_gbs / hbm_peak, 4), "traffic": args.traffic,
+                         "frac": round(achieved_gbs / hbm_peak, 4),
+                         "traffic": args.traffic if args.traffic is not None else round(TRAFFIC_6144 * (n / 6144) ** 2),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, mean of the "
+                                           "12 operators at 6144^2, scaled by the point count",
                          "peak_source": f"{hbm_src} hbm_gbs",
                          "note": "16 B/pt algorithmic; FP64 kernels are bound by the FP64 FMA pipe, see fp64"},
             "fp64": {"achieved_fma_s": round(achieved_fma / 1e9, 1), "peak_fma_s": round(fp64_rate / 1e9, 1),
@@ -861,7 +868,8 @@ def main():
     ap.add_argument("--skip-weno", action="store_true")
     ap.add_argument("--skip-indirect", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
-                    help="dram bytes per launch from an ncu capture (recorded in the roofline object)")
+                    help="dram bytes per launch from an ncu capture (default: the 6144^2 capture in "
+                         "profiles/stencil_sweep_traffic.md scaled to --n)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
