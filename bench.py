@@ -346,6 +346,9 @@ def run_gpu(args, world, rank, local):
     import custen_gb300 as cs
 
     cs.build()
+    # Kernel configurations: tuned at each handle's first (warm-up) Compute and cached (autotune.cu)
+    cs.set_tune_cache(str(ROOT / "_build" / f"tune_cache_rank{rank}.json"))
+    cs.set_autotune(args.autotune)
     torch.cuda.set_device(local)
     cs._check(cs.lib().custen_set_device(local))
     dev = torch.device("cuda", local)
@@ -433,6 +436,7 @@ def run_gpu(args, world, rank, local):
     for (nm, v, *_rest), ms in zip(ops, per_op):
         dfma_pt = _rest[-1]
         per[nm] = {"gpts_s": round(n * n / (ms * 1e-3) / 1e9, 3), "ms": round(ms, 4),
+                   "config": hs64[len(per)].config(),
                    "hbm_gbs": round(16.0 * n * n / (ms * 1e-3) / 1e9, 1),
                    "fp64_frac": round(dfma_pt * n * n / (ms * 1e-3) / fp64_rate, 3)}
 
@@ -462,10 +466,10 @@ def run_gpu(args, world, rank, local):
         ms32, per32, _ = timed_sweep(hs32, max(1, args.steps), 3)
         fp32 = {"gpts_s": round(pts_step / (ms32 / max(1, args.steps) * 1e-3) / 1e9, 3),
                 "hbm_gbs": round(8.0 * pts_step / (sum(per32) * 1e-3) / 1e9, 1), "per_op": {}}
-        for (nm, *_r), ms, o32, o64 in zip(ops, per32, outs32, outs64):
+        for (nm, *_r), ms, o32, o64, h32 in zip(ops, per32, outs32, outs64, hs32):
             d = o32.double() - o64
             fp32["per_op"][nm] = {
-                "gpts_s": round(n * n / (ms * 1e-3) / 1e9, 3),
+                "gpts_s": round(n * n / (ms * 1e-3) / 1e9, 3), "config": h32.config(),
                 "gbs": round(8.0 * n * n / (ms * 1e-3) / 1e9, 1),
                 "max_abs_err": float(d.abs().max().item()),
                 "rel_l2": float((d.norm() / o64.norm()).item()),
@@ -867,6 +871,8 @@ def main():
     ap.add_argument("--skip-sizes", action="store_true")
     ap.add_argument("--skip-weno", action="store_true")
     ap.add_argument("--skip-indirect", action="store_true")
+    ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],
+                    help="kernel configuration choice: 0 defaults, 1 tune at the first Compute (default), 2 always")
     ap.add_argument("--traffic", type=float, default=None,
                     help="dram bytes per launch from an ncu capture (default: the 6144^2 capture in "
                          "profiles/stencil_sweep_traffic.md scaled to --n)")

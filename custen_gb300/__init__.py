@@ -27,6 +27,7 @@ XYWENOADVP = 12   # WENO5 advection, periodic (WenoAdvection)
 F64, F32 = 0, 1
 DEVICE, HOST = 0, 1
 HANDLE_BYTES = 200
+NUM_CONFIGS = 5   # kernel configurations per element type (stencil_configs.h)
 
 _lib = None
 
@@ -55,6 +56,14 @@ def lib() -> ctypes.CDLL:
         L.custen_transfer_bytes.restype = None
         L.custen_set_stage_chunk_bytes.argtypes = [sz]
         L.custen_set_stage_chunk_bytes.restype = None
+        L.custen_set_autotune.argtypes = [i]
+        L.custen_set_autotune.restype = None
+        L.custen_set_tune_cache.argtypes = [ctypes.c_char_p]
+        L.custen_set_tune_cache.restype = None
+        L.custen_tune_cache_path.argtypes = [ctypes.c_char_p, sz]
+        L.custen_autotune.argtypes = [vp, i]
+        L.custen_handle_config.argtypes = [vp, ctypes.c_char_p, sz]
+        L.custen_set_config.argtypes = [vp, i]
         L.custen_set_fun_fusion.argtypes = [i]
         L.custen_set_fun_fusion.restype = None
         L.custen_builtin_fun_id.argtypes = [vp, i]
@@ -152,6 +161,23 @@ def transfer_bytes() -> tuple:
     return int(h2d.value), int(d2h.value)
 
 
+def set_autotune(mode: int) -> None:
+    """0: cached configurations only (default); 1: tune launch geometries missing from the cache at a
+    handle's first Compute; 2: always tune."""
+    lib().custen_set_autotune(int(mode))
+
+
+def set_tune_cache(path) -> None:
+    """JSON file of tuned configurations (None: CUSTEN_TUNE_CACHE or ~/.cache/custen_gb300/tune.json)."""
+    lib().custen_set_tune_cache(None if path is None else str(path).encode())
+
+
+def tune_cache_path() -> str:
+    buf = ctypes.create_string_buffer(4096)
+    _check(lib().custen_tune_cache_path(buf, 4096))
+    return buf.value.decode()
+
+
 def set_fun_fusion(enable: bool) -> None:
     """Fused path for the library's own c^3 - c Fun functions (default on); off = indirect calls."""
     lib().custen_set_fun_fusion(int(bool(enable)))
@@ -206,6 +232,21 @@ class Stencil:
         if self._alive:
             self._alive = False
             _check(lib().custen_destroy(self.handle))
+
+    def autotune(self, reps: int = 3) -> str:
+        """Time every kernel configuration on this handle's launch now, cache the fastest, use it."""
+        _check(lib().custen_autotune(self.handle, reps))
+        return self.config()
+
+    def set_config(self, index: int) -> None:
+        """Pin this handle to kernel configuration `index` (-1: choose again at the next Compute)."""
+        _check(lib().custen_set_config(self.handle, int(index)))
+
+    def config(self) -> str:
+        """Name of the kernel configuration this handle uses."""
+        buf = ctypes.create_string_buffer(64)
+        _check(lib().custen_handle_config(self.handle, buf, 64))
+        return buf.value.decode()
 
     def field(self, name: str):
         """Read a cuSten_t field by name (layout of cuSten/src/struct/cuSten_struct_type.h:84-122)."""

@@ -29,10 +29,16 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
-# Translation units of the static drop-in library (the reference's libcuSten.a surface).
-LIB_SOURCES = ["plan.cu", "stencil_f64.cu", "stencil_f32.cu", "weno.cu"]
+# stencil_cfg.cu is compiled once per entry of the configuration table (stencil_configs.h).
+NUM_CONFIGS = 5
+CFG_UNITS = [(f"stencil_cfg_{d}_{k}", "stencil_cfg.cu", [f"-DCUSTEN_CFG_DTYPE={d}", f"-DCUSTEN_CFG_INDEX={k}"])
+             for d in (0, 1) for k in range(NUM_CONFIGS)]
+# Translation units of the static drop-in library (the reference's libcuSten.a surface):
+# (object name, source, extra flags).
+LIB_UNITS = [("plan", "plan.cu", []), ("stencil_dispatch", "stencil_dispatch.cu", []), ("weno", "weno.cu", []),
+             ("autotune", "autotune.cu", [])] + CFG_UNITS
 # Extra translation units of the shared library.
-SO_SOURCES = ["builtin_funs.cu", "probe.cu", "ch_solver.cu", "ch_server.cu"]
+SO_UNITS = [(Path(s).stem, s, []) for s in ("builtin_funs.cu", "probe.cu", "ch_solver.cu", "ch_server.cu")]
 
 
 def nvcc() -> str:
@@ -63,27 +69,28 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     BUILD.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
-    srcs = LIB_SOURCES + SO_SOURCES
-    objs = {s: BUILD / (Path(s).stem + ".o") for s in srcs}
+    units = LIB_UNITS + SO_UNITS
+    objs = {name: BUILD / (name + ".o") for name, _, _ in units}
 
-    def compile_one(src: str) -> None:
-        out = objs[src]
+    def compile_one(unit) -> None:
+        name, src, extra = unit
+        out = objs[name]
         if _needs(out, [CSRC / src] + hdrs):
-            cmd = [cc, *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(out)]
+            cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(CSRC / src), "-o", str(out)]
             if verbose:
                 print(" ".join(cmd), flush=True)
             _run(cmd)
 
-    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
-        list(ex.map(compile_one, srcs))
+    with cf.ThreadPoolExecutor(max_workers=jobs or max(1, min(16, os.cpu_count() or 1, len(units)))) as ex:
+        list(ex.map(compile_one, units))
 
-    all_objs = [str(objs[s]) for s in srcs]
-    if _needs(SO_PATH, [objs[s] for s in srcs]):
+    all_objs = [str(objs[name]) for name, _, _ in units]
+    if _needs(SO_PATH, list(objs.values())):
         tmp = SO_PATH.with_suffix(".so.tmp")
         _run([cc, *ARCH, "-shared", "-rdc=true", "-Xcompiler", "-fPIC", *all_objs, "-o", str(tmp), "-cudart",
               "static"])
         os.replace(tmp, SO_PATH)
-    lib_objs = [objs[s] for s in LIB_SOURCES]
+    lib_objs = [objs[name] for name, _, _ in LIB_UNITS]
     if _needs(A_PATH, lib_objs):
         tmp = A_PATH.with_suffix(".a.tmp")
         if tmp.exists():

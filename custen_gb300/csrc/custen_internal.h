@@ -130,6 +130,7 @@ struct PlanPrivate {
     // it can run as c^3 - c followed by plain weights (StencilArgs::pre).
     void* fused_func;
     int fused_pre;
+    int cfg;   // kernel configuration (stencil_configs.h) of the device-resident launches; -1 not chosen yet
     // Host-resident fields (pinned or system memory) are streamed through device staging slots:
     // kStageSlots slots of (T + chunk + B) input rows and chunk output rows, plus the weights.
     // Allocated at the first such Compute, freed by Destroy.

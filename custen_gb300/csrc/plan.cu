@@ -20,6 +20,7 @@
 #include "../../include/cuSten.h"
 #include "../../include/custen_gb300.h"
 #include "custen_internal.h"
+#include "stencil_configs.h"
 
 static_assert(sizeof(cuSten_t) == 200, "cuSten_t must keep the reference layout (200 bytes)");
 static_assert(offsetof(cuSten_t, weights) == 104, "cuSten_t::weights offset");
@@ -170,6 +171,7 @@ int create_plan(cuSten_t* h, int variant, int dtype, int dev, int numTiles, int 
     p.launches = 0;
     p.fused_func = nullptr;
     p.fused_pre = 0;
+    p.cfg = -1;
     p.stage = nullptr;
     p.stage_slot_bytes = 0;
     p.stage_rows = 0;
@@ -340,8 +342,7 @@ static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 
 static cudaError_t launch(const StencilArgs& a, int dtype, cudaStream_t s, PlanPrivate* p) {
     int path = 0;
     cudaError_t e = a.variant == V_XYWENOADVP ? launch_weno_adv(a, s)
-                    : dtype == DT_F64        ? launch_stencil_f64(a, s, &path)
-                                             : launch_stencil_f32(a, s, &path);
+                                             : launch_stencil_cfg(a, dtype, p->cfg < 0 ? 0 : p->cfg, s, &path);
     if (e == cudaSuccess) {
         ++p->launches;
         g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -617,7 +618,11 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
         return compute_staged(h, p, a, s, copy_s, s_out);
     }
     if (kind != 1) {
-        // Device-resident data: no copies.
+        // Device-resident data: no copies. The first Compute picks the kernel configuration (autotune.cu).
+        if (p->cfg < 0 && p->variant != V_XYWENOADVP) {
+            fill_launch(0, contiguous ? nt : 1);
+            p->cfg = choose_config(a, p->dtype, s, p->cfg == -2, 3);
+        }
         if (contiguous) {
             fill_launch(0, nt);
             CU_TRY(launch(a, p->dtype, s, p), "Computing stencil");
@@ -805,6 +810,39 @@ const char* custen_last_error(void) { return g_last_error.c_str(); }
 unsigned long long custen_kernel_launches(void) { return g_launches.load(); }
 unsigned long long custen_kernel_launches_tma(void) { return g_launches_tma.load(); }
 void custen_set_fun_fusion(int enable) { g_fun_fusion.store(enable ? 1 : 0); }
+void custen_set_autotune(int mode) { set_autotune_mode(mode); }
+void custen_set_tune_cache(const char* path) { set_tune_cache(path); }
+int custen_tune_cache_path(char* buf, size_t len) {
+    const std::string p = tune_cache_path();
+    if (!buf || len == 0) return fail_arg("buffer is NULL");
+    snprintf(buf, len, "%s", p.c_str());
+    return ST_OK;
+}
+int custen_autotune(cuSten_t* h, int reps) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    if (p->variant == V_XYWENOADVP) return fail_arg("the WENO operator has a single kernel configuration");
+    CU_TRY(cudaSetDevice(h->deviceNum), "Setting current device");
+    if (memory_kind(h->dataInput[0]) != 0 || memory_kind(h->dataOutput[0]) != 0)
+        return fail_arg("autotuning needs device-resident fields");
+    (void)reps;
+    p->cfg = -2;   // the next Compute tunes its launch geometry, whatever the mode and the cache hold
+    return compute_plan(h, DEVICE, nullptr);
+}
+int custen_set_config(cuSten_t* h, int index) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    if (index < -1 || index >= kNumConfigs) return fail_arg("configuration index %d out of range", index);
+    p->cfg = index;   // -1: choose again at the next Compute
+    return ST_OK;
+}
+int custen_handle_config(const cuSten_t* h, char* name, size_t len) {
+    PlanPrivate* p = priv_of(h);
+    if (!p) return fail_arg("cuSten handle was not created by this library (or was destroyed)");
+    if (!name || len == 0) return fail_arg("buffer is NULL");
+    snprintf(name, len, "%s", p->variant == V_XYWENOADVP ? "weno_tw64_th32" : config_name(p->dtype, p->cfg < 0 ? 0 : p->cfg));
+    return ST_OK;
+}
 void custen_set_stage_chunk_bytes(size_t bytes) { g_stage_chunk_bytes.store(bytes ? bytes : (size_t)32 << 20); }
 void custen_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h) {
     if (h2d) *h2d = g_h2d_bytes.load();

@@ -19,20 +19,26 @@
 
 namespace custen {
 
-template <typename T> struct VecT;
-template <> struct VecT<double> { using type = double2; static constexpr int n = 2; };
-template <> struct VecT<float> { using type = float4; static constexpr int n = 4; };
+// VEC adjacent outputs per thread, moved with one VEC-wide load / store. The halo columns of a staged
+// row are padded to 16 bytes whatever VEC is: a TMA box starts and spans whole 16-byte units.
+template <typename T, int N> struct VecN;
+template <> struct VecN<double, 1> { using type = double; };
+template <> struct VecN<double, 2> { using type = double2; };
+template <> struct VecN<float, 1> { using type = float; };
+template <> struct VecN<float, 2> { using type = float2; };
+template <> struct VecN<float, 4> { using type = float4; };
+template <typename T> struct Pad16 { static constexpr int n = 16 / (int)sizeof(T); };
 
 __host__ __device__ constexpr int round_up_int(int v, int m) { return (v + m - 1) / m * m; }
 
 // Geometry of the staged window, identical on host (shared-memory sizing) and device.
 template <typename T, int TW, int TH>
 struct TileGeom {
-    static constexpr int VEC = VecT<T>::n;
+    static constexpr int PAD = Pad16<T>::n;
     int LP, RP, SW, SR;
     __host__ __device__ TileGeom(const StencilArgs& a) {
-        LP = round_up_int(a.L, VEC);
-        RP = round_up_int(a.R, VEC);
+        LP = round_up_int(a.L, PAD);
+        RP = round_up_int(a.R, PAD);
         SW = LP + TW + RP;
         SR = TH + a.T + a.B;
     }
@@ -98,11 +104,10 @@ __device__ __forceinline__ void apply_cube(T* tile, int count, int tid) {
 }
 
 // Plain-load staging of the window (16-byte vector loads where the whole vector is in range).
-template <typename T, int TW, int TH, int NT>
+template <typename T, int TW, int TH, int NT, int VEC>
 __device__ __forceinline__ void stage_tile_ldg(const StencilArgs& a, T* tile, const TileGeom<T, TW, TH>& g,
                                                int x0, int y0, int tid) {
-    constexpr int VEC = VecT<T>::n;
-    using V = typename VecT<T>::type;
+    using V = typename VecN<T, VEC>::type;
     const int cvecs = g.SW / VEC;
     const int total = g.SR * cvecs;
     for (int e = tid; e < total; e += NT) {
@@ -160,11 +165,10 @@ template <typename T> using FunXY = T (*)(T*, T*, int, int, int, int);
 
 // Store VEC x RPT outputs of one thread: 16-byte vector stores where every point is written with its
 // stencil value, the reference's write rules (untouched / zero) elsewhere.
-template <typename T, int RPT>
-__device__ __forceinline__ void store_outputs(const StencilArgs& a, const T (&acc)[RPT][VecT<T>::n], int gx, int gy0,
+template <typename T, int RPT, int VEC>
+__device__ __forceinline__ void store_outputs(const StencilArgs& a, const T (&acc)[RPT][VEC], int gx, int gy0,
                                               bool all_write_tile) {
-    constexpr int VEC = VecT<T>::n;
-    using V = typename VecT<T>::type;
+    using V = typename VecN<T, VEC>::type;
 #pragma unroll
     for (int rr = 0; rr < RPT; ++rr) {
         const int gyl = gy0 + rr;
@@ -202,12 +206,10 @@ __device__ __forceinline__ void store_outputs(const StencilArgs& a, const T (&ac
 }
 
 // Compute VEC x RPT outputs per thread from the staged window and store them.
-template <typename T, int TW, int TH, int RPT>
+template <typename T, int TW, int TH, int RPT, int VEC>
 __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile, T* coef_s, const int* list_off,
                                                   const T* list_w, int nlist, const TileGeom<T, TW, TH>& g,
                                                   int x0, int y0, int tx, int ty, bool is_fun, bool all_write_tile) {
-    constexpr int VEC = VecT<T>::n;
-    using V = typename VecT<T>::type;
     const int c0 = tx * VEC;    // tile-local column of the first output
     const int r0 = ty * RPT;    // tile-local row of the first output
     T acc[RPT][VEC];
@@ -245,7 +247,7 @@ __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile,
         }
     }
 
-    store_outputs<T, RPT>(a, acc, x0 + c0, y0 + r0, all_write_tile);
+    store_outputs<T, RPT, VEC>(a, acc, x0 + c0, y0 + r0, all_write_tile);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -281,13 +283,12 @@ inline int shape_mode(int H, int L, int V, int T) {
 // the columns its VEC outputs need) and applied to every output row whose window contains it. Per
 // output the FMAs run j = 0..V-1 (rows, top first), i = 0..H-1 -- the reference order
 // (2d_xy_p_kernel.cu:507-520) -- all weights included, zeros too.
-template <typename T, int TW, int TH, int RPT, class SH>
+template <typename T, int TW, int TH, int RPT, int VEC, class SH>
 __device__ __forceinline__ void compute_window_store(const StencilArgs& a, const T* tile, const T* coef_s,
                                                      const TileGeom<T, TW, TH>& g, int x0, int y0, int tx, int ty,
                                                      bool all_write_tile) {
-    constexpr int VEC = VecT<T>::n;
-    using VV = typename VecT<T>::type;
-    constexpr int LP = round_up_int(SH::L, VEC);
+    using VV = typename VecN<T, VEC>::type;
+    constexpr int LP = round_up_int(SH::L, Pad16<T>::n);
     constexpr int D = LP - SH::L;                       // first needed column inside the aligned segment
     constexpr int NV = (D + VEC + SH::H - 1 + VEC - 1) / VEC;
     const int c0 = tx * VEC, r0 = ty * RPT;
@@ -319,7 +320,7 @@ __device__ __forceinline__ void compute_window_store(const StencilArgs& a, const
             }
         }
     }
-    store_outputs<T, RPT>(a, acc, x0 + c0, y0 + r0, all_write_tile);
+    store_outputs<T, RPT, VEC>(a, acc, x0 + c0, y0 + r0, all_write_tile);
 }
 
 }  // namespace custen

@@ -12,10 +12,9 @@
 namespace custen {
 
 // Plain-load staged kernel: handles every geometry (odd widths, unaligned rows, any halo).
-template <typename T, int TW, int TH, int RPT>
-__global__ void __launch_bounds__((TW / VecT<T>::n) * (TH / RPT))
+template <typename T, int TW, int TH, int RPT, int VEC>
+__global__ void __launch_bounds__((TW / VEC) * (TH / RPT), min_blocks_for((TW / VEC) * (TH / RPT), true))
 stencil_ldg_kernel(const __grid_constant__ StencilArgs a) {
-    constexpr int VEC = VecT<T>::n;
     constexpr int NTX = TW / VEC;
     constexpr int NT = NTX * (TH / RPT);
     extern __shared__ __align__(16) unsigned char smem[];
@@ -27,15 +26,15 @@ stencil_ldg_kernel(const __grid_constant__ StencilArgs a) {
     const int tid = threadIdx.x + threadIdx.y * NTX;
     const bool is_fun = variant_is_fun(a.variant) && !a.pre;
     const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
-    stage_tile_ldg<T, TW, TH, NT>(a, tile, g, x0, y0, tid);
+    stage_tile_ldg<T, TW, TH, NT, VEC>(a, tile, g, x0, y0, tid);
     const int nlist = stage_coefficients<T, NT>(a, coef_s, list_off, list_w, g.SW, tid, is_fun);  // syncs
     if (a.pre) {
         apply_cube<T, NT>(tile, g.SR * g.SW, tid);
         __syncthreads();
     }
     const bool all_write = tile_all_write(a, x0, x0 + TW, a.row0 + y0, a.row0 + y0 + TH);
-    compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
-                                      threadIdx.y, is_fun, all_write);
+    compute_and_store<T, TW, TH, RPT, VEC>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
+                                           threadIdx.y, is_fun, all_write);
 }
 
 // Largest dynamic shared memory a block may opt in to on the current device.
@@ -57,16 +56,15 @@ inline cudaError_t ensure_smem(Kernel k, size_t smem) {
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-template <typename T, int TW, int TH, int RPT>
+template <typename T, int TW, int TH, int RPT, int VEC>
 cudaError_t launch_ldg(const StencilArgs& a, cudaStream_t s) {
-    constexpr int VEC = VecT<T>::n;
     TileGeom<T, TW, TH> g(a);
     const size_t smem = g.total_bytes(a);
-    cudaError_t e = ensure_smem(stencil_ldg_kernel<T, TW, TH, RPT>, smem);
+    cudaError_t e = ensure_smem(stencil_ldg_kernel<T, TW, TH, RPT, VEC>, smem);
     if (e != cudaSuccess) return e;
     dim3 block(TW / VEC, TH / RPT);
     dim3 grid((a.nx + TW - 1) / TW, (a.rows + TH - 1) / TH);
-    stencil_ldg_kernel<T, TW, TH, RPT><<<grid, block, smem, s>>>(a);
+    stencil_ldg_kernel<T, TW, TH, RPT, VEC><<<grid, block, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -115,9 +113,8 @@ inline int sm_count() {
 }
 
 // TMA path: returns cudaErrorNotSupported (without launching) when the geometry does not allow it.
-template <typename T, int TW, int TH, int RPT, int S, int MODE>
+template <typename T, int TW, int TH, int RPT, int VEC, int S, int MODE>
 cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
-    constexpr int VEC = VecT<T>::n;
     TileGeom<T, TW, TH> g(a);
     // One box per window: at most 256 columns and 256 rows; rows and columns tile exactly; rows
     // 16-byte aligned (global address and stride rules of cuTensorMapEncodeTiled).
@@ -129,7 +126,7 @@ cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
     const size_t smem = S * stage_bytes + round_up_int(a.ncoef * (int)sizeof(T), 16) +
                         round_up_int(a.ncoef * (int)sizeof(int), 16) + round_up_int(a.ncoef * (int)sizeof(T), 16) +
                         256;   // 128 bytes of alignment slack for the ring base + tail padding
-    auto kern = stencil_tma_kernel<T, TW, TH, RPT, S, MODE>;
+    auto kern = stencil_tma_kernel<T, TW, TH, RPT, VEC, S, MODE>;
     cudaError_t e = ensure_smem(kern, smem);
     if (e != cudaSuccess) return e == cudaErrorInvalidConfiguration ? cudaErrorNotSupported : e;
     int per_sm = 0;
@@ -143,20 +140,20 @@ cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <typename T, int TW, int TH, int RPT, int S>
+template <typename T, int TW, int TH, int RPT, int VEC, int S>
 cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
     const int mode = (variant_is_fun(a.variant) && !a.pre) ? (int)MODE_FUN : shape_mode(a.H, a.L, a.V, a.T);
     switch (mode) {
-    case MODE_FUN: return launch_tma_mode<T, TW, TH, RPT, S, MODE_FUN>(a, s);
-    case 2: return launch_tma_mode<T, TW, TH, RPT, S, 2>(a, s);
-    case 3: return launch_tma_mode<T, TW, TH, RPT, S, 3>(a, s);
-    case 4: return launch_tma_mode<T, TW, TH, RPT, S, 4>(a, s);
-    case 5: return launch_tma_mode<T, TW, TH, RPT, S, 5>(a, s);
-    case 6: return launch_tma_mode<T, TW, TH, RPT, S, 6>(a, s);
-    case 7: return launch_tma_mode<T, TW, TH, RPT, S, 7>(a, s);
-    case 8: return launch_tma_mode<T, TW, TH, RPT, S, 8>(a, s);
-    case 9: return launch_tma_mode<T, TW, TH, RPT, S, 9>(a, s);
-    default: return launch_tma_mode<T, TW, TH, RPT, S, MODE_LIST>(a, s);
+    case MODE_FUN: return launch_tma_mode<T, TW, TH, RPT, VEC, S, MODE_FUN>(a, s);
+    case 2: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 2>(a, s);
+    case 3: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 3>(a, s);
+    case 4: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 4>(a, s);
+    case 5: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 5>(a, s);
+    case 6: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 6>(a, s);
+    case 7: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 7>(a, s);
+    case 8: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 8>(a, s);
+    case 9: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 9>(a, s);
+    default: return launch_tma_mode<T, TW, TH, RPT, VEC, S, MODE_LIST>(a, s);
     }
 }
 

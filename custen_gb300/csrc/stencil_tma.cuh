@@ -122,11 +122,14 @@ __device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const 
 // MODE: MODE_LIST (weights, generic window), MODE_FUN (device function), or a compile-time shape.
 // FP64 shape kernels fall back to the list when a weight is zero (FP64 FMAs are the bottleneck on
 // GB300; dropping exact zeros is bit-neutral for finite inputs).
-template <typename T, int TW, int TH, int RPT, int S, int MODE>
-__global__ void __launch_bounds__((TW / VecT<T>::n) * (TH / RPT), MODE == MODE_FUN ? 2 : 3)
+// Resident CTAs the register allocation must allow: 768 threads per SM (512 for the device-function
+// mode, whose indirect calls need more registers).
+constexpr int min_blocks_for(int threads, bool fun) { return (fun ? 512 : 768) / threads > 0 ? (fun ? 512 : 768) / threads : 1; }
+
+template <typename T, int TW, int TH, int RPT, int VEC, int S, int MODE>
+__global__ void __launch_bounds__((TW / VEC) * (TH / RPT), min_blocks_for((TW / VEC) * (TH / RPT), MODE == MODE_FUN))
 stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__ StencilArgs a, int tiles_x,
                    int tiles_total) {
-    constexpr int VEC = VecT<T>::n;
     constexpr int NTX = TW / VEC;
     constexpr int NT = NTX * (TH / RPT);
     // The dynamic segment is only guaranteed 16-byte alignment (with relocatable device code its
@@ -200,14 +203,14 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
         if constexpr (MODE >= MODE_FIRST_SHAPE) {
             using SH = typename ShapeOf<MODE>::type;
             if (sizeof(T) == 4 || nlist == SH::H * SH::V)
-                compute_window_store<T, TW, TH, RPT, SH>(a, tile, coef_s, g, x0, y0, threadIdx.x, threadIdx.y,
-                                                         all_write);
+                compute_window_store<T, TW, TH, RPT, VEC, SH>(a, tile, coef_s, g, x0, y0, threadIdx.x,
+                                                              threadIdx.y, all_write);
             else
-                compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0,
-                                                  threadIdx.x, threadIdx.y, false, all_write);
+                compute_and_store<T, TW, TH, RPT, VEC>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0,
+                                                       threadIdx.x, threadIdx.y, false, all_write);
         } else {
-            compute_and_store<T, TW, TH, RPT>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
-                                              threadIdx.y, is_fun, all_write);
+            compute_and_store<T, TW, TH, RPT, VEC>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
+                                                   threadIdx.y, is_fun, all_write);
         }
         fence_proxy_async_smem();
         __syncthreads();   // every thread is done with stage s

@@ -49,6 +49,22 @@ void custen_set_stage_chunk_bytes(size_t bytes);
  * coefficients as plain weights: bit-identical results, fewer FP64 operations. enable = 0 sends them
  * through the indirect call like any user function. Default 1. No reference counterpart. */
 void custen_set_fun_fusion(int enable);
+/* ---- autotuner (no reference counterpart) ----
+ * The stencil kernels come in several tile configurations (tile width / height, rows per thread, vector
+ * width: the role of BLOCK_X / BLOCK_Y); all compute identical values. A handle's first Compute on
+ * device-resident fields picks one: mode 0 looks the launch geometry up in the JSON cache and uses the
+ * default when absent (default mode); mode 1 also tunes absent geometries (times every configuration on
+ * that launch) and stores the result; mode 2 always tunes. The environment variable CUSTEN_AUTOTUNE sets
+ * the initial mode; the cache file is custen_set_tune_cache's path, else CUSTEN_TUNE_CACHE, else
+ * $HOME/.cache/custen_gb300/tune.json. custen_autotune tunes one handle now. */
+void custen_set_autotune(int mode);
+void custen_set_tune_cache(const char* path);
+int custen_tune_cache_path(char* buf, size_t len);
+int custen_autotune(cuSten_t* h, int reps);
+int custen_handle_config(const cuSten_t* h, char* name, size_t len);
+/* Pin a handle to configuration `index` (0 .. 4; -1: choose again at the next Compute). */
+int custen_set_config(cuSten_t* h, int index);
+
 /* Which shipped function (0..5) `f` is on the current device, or -1. */
 int custen_builtin_fun_id(const void* f, int dtype);
 

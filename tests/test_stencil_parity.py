@@ -28,7 +28,7 @@ def geometry(variant, kind):
 
 
 def run_both(variant, nx, ny, tiles, bx, by, geom, dtype=np.float64, fun_id=-1, seed=0, managed=False,
-             offload=cs.DEVICE, mem=None):
+             offload=cs.DEVICE, mem=None, config=None):
     """mem: "device" (default), "managed", "pinned" (cudaMallocHost) or "pageable" (numpy memory)."""
     mem = mem or ("managed" if managed else "device")
     H, L, R, V, T, B = geom
@@ -60,6 +60,8 @@ def run_both(variant, nx, ny, tiles, bx, by, geom, dtype=np.float64, fun_id=-1, 
     func = cs.builtin_function(fun_id, dt) if fun else None
     s = cs.Stencil(variant, nx, ny, ptrs[0], ptrs[1], ptrs[2], H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=tiles,
                    block_x=bx, block_y=by, dtype=dt, ncoef=ncoef, func=func)
+    if config is not None:
+        s.set_config(config)
     s.compute(offload)
     cs._check(cs.lib().custen_device_synchronize())
     if mem == "device":
