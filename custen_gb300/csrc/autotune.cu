@@ -133,7 +133,7 @@ std::string gpu_name() {
 
 std::string make_key(const StencilArgs& a, int dtype) {
     char buf[256];
-    snprintf(buf, sizeof(buf), "|v%d|%s|%dx%d|%d.%d.%d.%d.%d.%d|pre%d|vec%d", a.variant, dtype == DT_F64 ? "f64" : "f32",
+    snprintf(buf, sizeof(buf), "|v%d|%s|%dx%d|%d.%d.%d.%d.%d.%d|pre%d|aligned%d", a.variant, dtype == DT_F64 ? "f64" : "f32",
              a.nx, a.rows, a.H, a.L, a.R, a.V, a.T, a.B, a.pre, a.vec_ok);
     return gpu_name() + buf;
 }
