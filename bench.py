@@ -773,6 +773,7 @@ def run_ch_batched(args, cs):
             b.set_state(k, crng.uniform(-0.1, 0.1, (n, n)))
         b.step(2)
         b.synchronize()
+        cfg_name = b.autotune(steps=4) if args.autotune else b.config()   # state restored by the tuner
         l0 = b.launches()
         t0 = time.perf_counter()
         b.step(steps)
@@ -781,7 +782,7 @@ def run_ch_batched(args, cs):
         out[label] = {"wall_s": round(wall, 4), "steps_per_s": round(len(sizes) * steps / wall, 1),
                       "gpt_steps_per_s": round(out["points"] * steps / wall / 1e9, 3),
                       "ms_per_step": round(wall / steps * 1e3, 4), "launches": b.launches() - l0,
-                      "graphs": "pairs of steps"}
+                      "graphs": "pairs of steps", "kernel_config": cfg_name}
         b.close()
     # plain loop on the same GPU: one grid at a time (per-size step time measured, then summed)
     per_size = {n: plain_step_seconds(cs, n) for n in sorted(set(sizes))}

@@ -98,6 +98,9 @@ def lib() -> ctypes.CDLL:
         L.custen_ch_batch_launches.argtypes = [vp]
         L.custen_ch_batch_launches.restype = ull
         L.custen_ch_batch_destroy.argtypes = [vp]
+        L.custen_ch_batch_autotune.argtypes = [vp, i, ctypes.c_char_p, sz]
+        L.custen_ch_batch_config.argtypes = [vp, ctypes.c_char_p, sz]
+        L.custen_ch_batch_set_config.argtypes = [vp, i]
         L.custen_ch_server_last_error.restype = ctypes.c_char_p
         L.custen_ch_server_create.argtypes = [ctypes.POINTER(vp), ctypes.c_double, i, ctypes.c_double, ctypes.c_double,
                                               i, i]
@@ -352,6 +355,21 @@ class CahnHilliardBatch:
 
     def step(self, steps: int = 1, graph: bool = True) -> None:
         _ch_check(lib().custen_ch_batch_step(self.h, steps, int(graph)))
+
+    def autotune(self, steps: int = 4) -> str:
+        """Time every kernel configuration on this batch (state restored afterwards); keep the fastest."""
+        buf = ctypes.create_string_buffer(64)
+        _ch_check(lib().custen_ch_batch_autotune(self.h, int(steps), buf, 64))
+        return buf.value.decode()
+
+    def config(self) -> str:
+        buf = ctypes.create_string_buffer(64)
+        _ch_check(lib().custen_ch_batch_config(self.h, buf, 64))
+        return buf.value.decode()
+
+    def set_config(self, index: int) -> None:
+        """Pin the kernel configuration (0 .. 5; -1: the default)."""
+        _ch_check(lib().custen_ch_batch_set_config(self.h, int(index)))
 
     def synchronize(self) -> None:
         _ch_check(lib().custen_ch_batch_synchronize(self.h))

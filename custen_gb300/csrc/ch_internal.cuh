@@ -34,14 +34,25 @@ struct Item {
     int block;   // K1: 32 x 32 block index (row-major over the grid); K2: row block; K3: column block
 };
 
-template <typename T>
-__global__ void ch_rhs_kernel(const GridDev* __restrict__ grids, const Item* __restrict__ items, int n_items, int parity,
-                              unsigned int* counter);
 __global__ void ch_xsolve_kernel(const GridDev* __restrict__ grids, const Item* __restrict__ items, int n_items,
                                  unsigned int* counter);
-__global__ void ch_ysolve_kernel(const GridDev* __restrict__ grids, const Item* __restrict__ items, int n_items,
-                                 int parity, unsigned int* counter);
 __global__ void ch_mass_kernel(const double* __restrict__ f, long long count, double* out);
+
+// Kernel configuration of a step: warps per right-hand-side CTA (1, 2, 4) and rows per batch of the y
+// sweep (16, 32). Every configuration computes the same values; the batch tuner times them.
+struct ChConfig {
+    int rhs_warps;
+    int y_chunk;
+};
+constexpr ChConfig kChDefault{4, 16};
+constexpr int kChConfigs = 6;
+ChConfig ch_config(int index);   // 0 .. kChConfigs-1
+
+// One step of every grid of a work list: right-hand side, x sweep, y sweep (3 launches on s).
+// counters: 3 zeroed work counters.
+cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grids, const Item* items_rhs, int n_rhs,
+                           const Item* items_rows, int n_rows, int parity, unsigned int* counters, int sms,
+                           cudaStream_t s);
 
 // Solver table of an n x n grid (tab_size(n) doubles) built on the host.
 std::vector<double> build_table(int n, double lx, double gamma, double dt_factor);

@@ -228,17 +228,9 @@ static int retire(Server* S, int id, double now_after) {
 static int enqueue_steps(Server* S, int k) {
     for (int s = 0; s < k; ++s) {
         SRV_TRY(cudaMemsetAsync(S->counters, 0, 3 * sizeof(unsigned int), S->stream), "Resetting counters");
-        const int g1 = std::min(S->n_rhs, S->sms * 16), g23 = std::min(S->n_rows, S->sms * 16);
-        if (S->rhs_fp32)
-            ch_rhs_kernel<float><<<g1, BLK, 0, S->stream>>>(S->grids_d, S->items_rhs_d, S->n_rhs, S->parity,
-                                                              S->counters);
-        else
-            ch_rhs_kernel<double><<<g1, BLK, 0, S->stream>>>(S->grids_d, S->items_rhs_d, S->n_rhs, S->parity,
-                                                               S->counters);
-        ch_xsolve_kernel<<<g23, BLK, 0, S->stream>>>(S->grids_d, S->items_rows_d, S->n_rows, S->counters + 1);
-        ch_ysolve_kernel<<<g23, BLK, 0, S->stream>>>(S->grids_d, S->items_rows_d, S->n_rows, S->parity,
-                                                       S->counters + 2);
-        SRV_TRY(cudaGetLastError(), "Launching a step");
+        SRV_TRY(launch_ch_step(kChDefault, S->rhs_fp32 != 0, S->grids_d, S->items_rhs_d, S->n_rhs, S->items_rows_d,
+                               S->n_rows, S->parity, S->counters, S->sms, S->stream),
+                "Launching a step");
         S->launches += 3;
         S->parity ^= 1;
     }

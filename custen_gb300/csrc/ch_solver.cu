@@ -52,19 +52,24 @@ namespace ch {
 // about 16 FP64 operations per point instead of 24 for the two stencils taken separately. The sums are
 // the same mathematically; their rounding differs from the reference's weight-by-weight chain at the
 // level of one rounding per term, far inside the solver's 1e-10 parity bar.
-template <typename T>
-__global__ void __launch_bounds__(BLK) ch_rhs_kernel(const GridDev* __restrict__ grids, const Item* __restrict__ items,
-                                                     int n_items, int parity, unsigned int* counter) {
+// NW warps per CTA share one 32 x 32 work item: shared memory limits residency to a few CTAs per SM, so
+// more warps per CTA give the FP64 pipe more warps to issue from (the tuned choice, ChConfig).
+template <typename T, int NW>
+__global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restrict__ grids,
+                                                          const Item* __restrict__ items, int n_items, int parity,
+                                                          unsigned int* counter) {
     __shared__ T cb[36][37];   // cBar over the block and a 2-point halo
     __shared__ T hh[34][35];   // sigma_nl * (c^3 - c), then h, over the block and a 1-point halo
     __shared__ T dco[32][33];  // cCurr - cOld at the block's points
     __shared__ int s_item;
-    const int lane = threadIdx.x;
+    constexpr int NT = NW * BLK;
+    const int tid = threadIdx.x;
+    const int lane = tid & (BLK - 1), warp = tid / BLK;
     for (;;) {
-        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
-        __syncwarp();
+        if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
         const int it = s_item;
-        __syncwarp();
+        __syncthreads();
         if (it >= n_items) break;
         const Item item = items[it];
         const GridDev gd = grids[item.grid];
@@ -81,7 +86,7 @@ __global__ void __launch_bounds__(BLK) ch_rhs_kernel(const GridDev* __restrict__
         const T s_nl = (T)tab[7 * m + 33 + 1];
         // stage the 36 x 36 window (periodic wrap)
 #pragma unroll 4
-        for (int e = lane; e < 36 * 36; e += BLK) {
+        for (int e = tid; e < 36 * 36; e += NT) {
             const int r = e / 36, c = e - r * 36;
             int gy = y0 - 2 + r, gx = x0 - 2 + c;
             gy = gy < 0 ? gy + n : (gy >= n ? gy - n : gy);
@@ -93,24 +98,24 @@ __global__ void __launch_bounds__(BLK) ch_rhs_kernel(const GridDev* __restrict__
             if (r >= 1 && r < 35 && c >= 1 && c < 35) hh[r - 1][c - 1] = s_nl * fma(c32 * c32, c32, -c32);
             if (r >= 2 && r < 34 && c >= 2 && c < 34) dco[r - 2][c - 2] = c32 - o32;
         }
-        __syncwarp();
+        __syncthreads();
         // h = sigma_nl * g - sigma_lin * Lap(cBar) over the 34 x 34 block + halo
 #pragma unroll 4
-        for (int e = lane; e < 34 * 34; e += BLK) {
+        for (int e = tid; e < 34 * 34; e += NT) {
             const int r = e / 34, c = e - r * 34;
             const T lap = fma((T)(-4), cb[r + 1][c + 1], (cb[r][c + 1] + cb[r + 2][c + 1]) + (cb[r + 1][c] + cb[r + 1][c + 2]));
             hh[r][c] = fma(-s_lin, lap, hh[r][c]);
         }
-        __syncwarp();
+        __syncthreads();
         // rhs = Lap(h) - (2/3)(cCurr - cOld)  (findRHS, cuPentCahnADI.cu:72-86); lane = column
         const int j = lane;
         double* out = gd.tmp + (size_t)y0 * n + x0 + j;
 #pragma unroll 4
-        for (int rr = 0; rr < BLK; ++rr) {
+        for (int rr = warp; rr < BLK; rr += NW) {
             const T lap = fma((T)(-4), hh[rr + 1][j + 1], (hh[rr][j + 1] + hh[rr + 2][j + 1]) + (hh[rr + 1][j] + hh[rr + 1][j + 2]));
             out[(size_t)rr * n] = (double)fma((T)(-2.0 / 3.0), dco[rr][j], lap);
         }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -238,6 +243,9 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
 // Rows are taken 32 at a time: the batch's field values are loaded into registers first (32 loads
 // in flight per lane) and the batch's table entries / row ends are loaded coalesced and broadcast
 // with shuffles, so the FP64 recurrence does not wait on memory.
+// CH rows per batch (16 or 32): the three CH-deep register arrays of the update set the register use,
+// hence how many warps fit on an SM (the tuned choice, ChConfig).
+template <int CH>
 __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restrict__ grids,
                                                         const Item* __restrict__ items, int n_items, int parity,
                                                         unsigned int* counter) {
@@ -268,18 +276,18 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
         const bool corr = x < m;
         const double cx1 = corr ? inv1[x] : 0.0;
         const double cx2 = corr ? inv2[x] : 0.0;
-        const int nb = n / BLK;
+        const int nb = n / CH;
         // forward elimination along y
         double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
         for (int bb = 0; bb < nb; ++bb) {
-            const int yb = bb * BLK, yl = yb + lane;
+            const int yb = bb * CH, yl = yb + lane;
             const double tds = yl < m ? ds[yl] : 0.0, tdl = yl < m ? dl[yl] : 0.0, trd = yl < m ? rd[yl] : 0.0;
-            const double e2 = ends[2 * yl], e1 = ends[2 * yl + 1];
-            double v[BLK];
+            const double e2 = yl < n ? ends[2 * yl] : 0.0, e1 = yl < n ? ends[2 * yl + 1] : 0.0;
+            double v[CH];
 #pragma unroll
-            for (int k = 0; k < BLK; ++k) v[k] = t[(size_t)(yb + k) * n + x];
+            for (int k = 0; k < CH; ++k) v[k] = t[(size_t)(yb + k) * n + x];
 #pragma unroll
-            for (int k = 0; k < BLK; ++k) {
+            for (int k = 0; k < CH; ++k) {
                 const int y = yb + k;
                 const double c2 = __shfl_sync(FULL, e2, k), c1 = __shfl_sync(FULL, e1, k);
                 const double a_s = __shfl_sync(FULL, tds, k), a_l = __shfl_sync(FULL, tdl, k);
@@ -299,19 +307,19 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
                 }
             }
 #pragma unroll
-            for (int k = 0; k < BLK; ++k)
+            for (int k = 0; k < CH; ++k)
                 if (yb + k < m) t[(size_t)(yb + k) * n + x] = v[k];
         }
         // backward substitution
         double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
         for (int bb = nb - 1; bb >= 0; --bb) {
-            const int yb = bb * BLK, yl = yb + lane;
+            const int yb = bb * CH, yl = yb + lane;
             const double tdu = yl < m ? du[yl] : 0.0, tdw = yl < m ? dw[yl] : 0.0;
-            double v[BLK];
+            double v[CH];
 #pragma unroll
-            for (int k = 0; k < BLK; ++k) v[k] = (yb + k < m) ? t[(size_t)(yb + k) * n + x] : 0.0;
+            for (int k = 0; k < CH; ++k) v[k] = (yb + k < m) ? t[(size_t)(yb + k) * n + x] : 0.0;
 #pragma unroll
-            for (int k = BLK - 1; k >= 0; --k) {
+            for (int k = CH - 1; k >= 0; --k) {
                 const int y = yb + k;
                 const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
                 if (y < m) {
@@ -327,7 +335,7 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
                 }
             }
 #pragma unroll
-            for (int k = 0; k < BLK; ++k)
+            for (int k = 0; k < CH; ++k)
                 if (yb + k < m) t[(size_t)(yb + k) * n + x] = v[k];
         }
         const double* om = tab + 7 * m;
@@ -340,18 +348,18 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
         const double* cur = parity ? gd.buf[1] : gd.buf[0];
         double* old = parity ? gd.buf[0] : gd.buf[1];
         for (int bb = 0; bb < nb; ++bb) {
-            const int yb = bb * BLK, yl = yb + lane;
+            const int yb = bb * CH, yl = yb + lane;
             const double ti1 = yl < m ? inv1[yl] : 0.0, ti2 = yl < m ? inv2[yl] : 0.0;
-            double v[BLK], cv[BLK], ov[BLK];
+            double v[CH], cv[CH], ov[CH];
 #pragma unroll
-            for (int k = 0; k < BLK; ++k) {
+            for (int k = 0; k < CH; ++k) {
                 const size_t q = (size_t)(yb + k) * n + x;
                 v[k] = (yb + k < m) ? t[q] : 0.0;
                 cv[k] = cur[q];
                 ov[k] = old[q];
             }
 #pragma unroll
-            for (int k = 0; k < BLK; ++k) {
+            for (int k = 0; k < CH; ++k) {
                 const int y = yb + k;
                 const double a1 = __shfl_sync(FULL, ti1, k), a2 = __shfl_sync(FULL, ti2, k);
                 double dlt;
@@ -362,6 +370,38 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
             }
         }
     }
+}
+
+ChConfig ch_config(int index) {
+    static const ChConfig tab[kChConfigs] = {{1, 32}, {2, 32}, {4, 32}, {1, 16}, {2, 16}, {4, 16}};
+    return tab[(index >= 0 && index < kChConfigs) ? index : 0];
+}
+
+template <typename T>
+static void launch_rhs(int nw, int grid, const GridDev* g, const Item* it, int n, int parity, unsigned int* ctr,
+                       cudaStream_t s) {
+    switch (nw) {
+    case 1: ch_rhs_kernel<T, 1><<<grid, BLK, 0, s>>>(g, it, n, parity, ctr); break;
+    case 4: ch_rhs_kernel<T, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr); break;
+    default: ch_rhs_kernel<T, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr); break;
+    }
+}
+
+cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grids, const Item* items_rhs, int n_rhs,
+                           const Item* items_rows, int n_rows, int parity, unsigned int* counters, int sms,
+                           cudaStream_t s) {
+    // persistent grids over the work lists; CTAs beyond the resident ones find the lists empty
+    const int g1 = std::max(1, std::min(n_rhs, sms * 32 / c.rhs_warps));
+    const int g23 = std::max(1, std::min(n_rows, sms * 16));
+    if (rhs_fp32) launch_rhs<float>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+    else launch_rhs<double>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    ch_xsolve_kernel<<<g23, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (c.y_chunk == 32) ch_ysolve_kernel<32><<<g23, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+    else ch_ysolve_kernel<16><<<g23, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+    return cudaGetLastError();
 }
 
 // Compensated (Neumaier) sum of one grid, one CTA of 256 threads; combined with a two-sum tree.
@@ -495,9 +535,12 @@ struct Batch {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};   // pair of steps starting at parity 0 / 1
-    int grid_k1 = 0, grid_k23 = 0;
+    int sms = 0;
+    int cfg = -1;   // ch_config index; -1: kChDefault
     unsigned long long launches = 0;
 };
+
+static ChConfig batch_config(const Batch* b) { return b->cfg < 0 ? kChDefault : ch_config(b->cfg); }
 
 static thread_local std::string g_ch_err;
 static int ch_fail(cudaError_t e, const char* what) {
@@ -518,17 +561,9 @@ static int ch_fail_arg(const std::string& msg) {
 static int enqueue_step(Batch* b, int parity, int slot) {
     unsigned int* ctr = b->counters + 3 * slot;
     CH_TRY(cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned int), b->stream), "Resetting work counters");
-    if (b->rhs_fp32)
-        ch_rhs_kernel<float><<<b->grid_k1, BLK, 0, b->stream>>>(b->grids_d, b->items_rhs, b->n_items_rhs, parity,
-                                                                ctr);
-    else
-        ch_rhs_kernel<double><<<b->grid_k1, BLK, 0, b->stream>>>(b->grids_d, b->items_rhs, b->n_items_rhs, parity,
-                                                                 ctr);
-    CH_TRY(cudaGetLastError(), "Launching right-hand side");
-    ch_xsolve_kernel<<<b->grid_k23, BLK, 0, b->stream>>>(b->grids_d, b->items_rows, b->n_items_rows, ctr + 1);
-    CH_TRY(cudaGetLastError(), "Launching x sweep");
-    ch_ysolve_kernel<<<b->grid_k23, BLK, 0, b->stream>>>(b->grids_d, b->items_rows, b->n_items_rows, parity, ctr + 2);
-    CH_TRY(cudaGetLastError(), "Launching y sweep");
+    CH_TRY(launch_ch_step(batch_config(b), b->rhs_fp32 != 0, b->grids_d, b->items_rhs, b->n_items_rhs, b->items_rows,
+                          b->n_items_rows, parity, ctr, b->sms, b->stream),
+           "Launching a step");
     return 0;
 }
 
@@ -664,11 +699,7 @@ int custen_ch_batch_create(void** out, int nsims, const int* n, const double* lx
     if (e == cudaSuccess) e = cudaMalloc(&b->counters, 6 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&b->mass_d, sizeof(double));
     if (e != cudaSuccess) return cleanup_fail(ch_fail(e, "Allocating work lists"));
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-    // one warp per CTA, enough CTAs to give every SM sub-partition several warps
-    b->grid_k1 = std::min(b->n_items_rhs, sms * 16);
-    b->grid_k23 = std::min(b->n_items_rows, sms * 16);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     *out = b;
     return 0;
 }
@@ -809,12 +840,107 @@ int custen_ch_step_noalloc(const double* c_old, const double* c_cur, double* c_n
     const Item* it_rows = reinterpret_cast<const Item*>(base + kNoAllocRowsOff);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    ch_rhs_kernel<double><<<std::min(bpr * bpr, sms * 16), BLK, 0, s>>>(gd, it_rhs, bpr * bpr, 0, ctr);
-    CH_TRY(cudaGetLastError(), "Launching right-hand side");
-    ch_xsolve_kernel<<<bpr, BLK, 0, s>>>(gd, it_rows, bpr, ctr + 1);
-    CH_TRY(cudaGetLastError(), "Launching x sweep");
-    ch_ysolve_kernel<<<bpr, BLK, 0, s>>>(gd, it_rows, bpr, 0, ctr + 2);
-    CH_TRY(cudaGetLastError(), "Launching y sweep");
+    CH_TRY(launch_ch_step(kChDefault, false, gd, it_rhs, bpr * bpr, it_rows, bpr, 0, ctr, sms, s), "Launching the step");
+    return 0;
+}
+
+// Kernel configuration of a batch: time every configuration (ch_config) over `steps` steps of the
+// batch itself, then restore the fields it started from, so tuning changes no result. Writes the
+// chosen configuration's name to `name`. No reference counterpart.
+int custen_ch_batch_autotune(void* h, int steps, char* name, size_t len) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || steps < 1) return ch_fail_arg("invalid arguments");
+    CH_TRY(cudaSetDevice(b->device), "Setting device");
+    size_t total = 0;
+    for (const auto& g : b->grids_h) total += (size_t)g.n * g.n;
+    double* save = nullptr;
+    CH_TRY(cudaMalloc(&save, 2 * total * sizeof(double)), "Allocating the saved state");
+    auto copy_state = [&](bool to_save) -> cudaError_t {
+        size_t off = 0;
+        for (const auto& g : b->grids_h) {
+            const size_t bytes = (size_t)g.n * g.n * sizeof(double);
+            for (int k = 0; k < 2; ++k) {
+                double* dev = g.buf[k];
+                double* sv = save + off;
+                cudaError_t e = cudaMemcpyAsync(to_save ? sv : dev, to_save ? dev : sv, bytes,
+                                                cudaMemcpyDeviceToDevice, b->stream);
+                if (e != cudaSuccess) return e;
+                off += (size_t)g.n * g.n;
+            }
+        }
+        return cudaSuccess;
+    };
+    const int parity0 = b->parity;
+    const long long done0 = b->steps_done;
+    const unsigned long long launches0 = b->launches;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = copy_state(true);
+    if (err == cudaSuccess) err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    int best = -1;
+    float best_ms = 0.f;
+    for (int c = 0; c < kChConfigs && err == cudaSuccess; ++c) {
+        b->cfg = c;
+        for (int p = 0; p < 2; ++p)
+            if (b->graph_exec[p]) {
+                cudaGraphExecDestroy(b->graph_exec[p]);
+                b->graph_exec[p] = nullptr;
+            }
+        if (custen_ch_batch_step(h, 2, 1) != 0) break;   // warm-up, graph capture
+        cudaEventRecord(e0, b->stream);
+        if (custen_ch_batch_step(h, steps, 1) != 0) break;
+        cudaEventRecord(e1, b->stream);
+        if ((err = cudaEventSynchronize(e1)) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best < 0 || ms < best_ms) {
+            best = c;
+            best_ms = ms;
+        }
+        if ((err = copy_state(false)) != cudaSuccess) break;
+        b->parity = parity0;
+        b->steps_done = done0;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(b->stream);
+    cudaFree(save);
+    b->parity = parity0;
+    b->steps_done = done0;
+    b->launches = launches0;
+    for (int p = 0; p < 2; ++p)
+        if (b->graph_exec[p]) {
+            cudaGraphExecDestroy(b->graph_exec[p]);
+            b->graph_exec[p] = nullptr;
+        }
+    if (err != cudaSuccess) return ch_fail(err, "Tuning the batch");
+    if (best < 0) return 1;
+    b->cfg = best;
+    if (name && len) {
+        const ChConfig c = ch_config(best);
+        snprintf(name, len, "rhs_warps%d_ychunk%d", c.rhs_warps, c.y_chunk);
+    }
+    return 0;
+}
+
+int custen_ch_batch_set_config(void* h, int index) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || index < -1 || index >= kChConfigs) return ch_fail_arg("invalid arguments");
+    CH_TRY(cudaStreamSynchronize(b->stream), "Synchronising the batch");
+    b->cfg = index;
+    for (int p = 0; p < 2; ++p)
+        if (b->graph_exec[p]) {
+            cudaGraphExecDestroy(b->graph_exec[p]);
+            b->graph_exec[p] = nullptr;
+        }
+    return 0;
+}
+
+int custen_ch_batch_config(void* h, char* name, size_t len) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || !name || !len) return ch_fail_arg("invalid arguments");
+    const ChConfig c = batch_config(b);
+    snprintf(name, len, "rhs_warps%d_ychunk%d", c.rhs_warps, c.y_chunk);
     return 0;
 }
 
@@ -838,10 +964,4 @@ int custen_ch_batch_destroy(void* h) {
 
 }  // extern "C"
 
-// Explicit instantiations for the other host translation units (the server).
-template __global__ void custen::ch::ch_rhs_kernel<double>(const custen::ch::GridDev* __restrict__,
-                                                           const custen::ch::Item* __restrict__, int, int,
-                                                           unsigned int*);
-template __global__ void custen::ch::ch_rhs_kernel<float>(const custen::ch::GridDev* __restrict__,
-                                                          const custen::ch::Item* __restrict__, int, int,
-                                                          unsigned int*);
+

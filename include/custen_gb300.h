@@ -176,6 +176,12 @@ int custen_ch_batch_step(void* batch, int steps, int use_graph);   /* asynchrono
 int custen_ch_batch_synchronize(void* batch);
 int custen_ch_batch_mean(void* batch, int sim, double* mean);     /* compensated FP64 sum */
 unsigned long long custen_ch_batch_launches(void* batch);
+/* Kernel configuration of the batch's steps (warps per right-hand-side CTA, rows per y-sweep batch):
+ * custen_ch_batch_autotune times every configuration over `steps` steps of the batch itself, restores
+ * the fields, and keeps the fastest; results do not depend on it. No reference counterpart. */
+int custen_ch_batch_autotune(void* batch, int steps, char* name, size_t len);
+int custen_ch_batch_config(void* batch, char* name, size_t len);
+int custen_ch_batch_set_config(void* batch, int index);   /* 0 .. 5; -1: the default */
 int custen_ch_batch_destroy(void* batch);
 
 /* ---- Cahn-Hilliard serving: request loop with continuous batching ----

@@ -109,3 +109,55 @@ def test_fp32_stencil_variant_error_reported(gpu):
     assert err < 1e-3
     assert drift < 1e-6
     b.close()
+
+
+CH_CONFIGS = 6
+
+
+def test_every_kernel_configuration_gives_identical_fields(gpu):
+    """The batch's kernel configurations (warps per right-hand-side CTA, y-sweep batch depth) compute
+    the same values: fields after 6 steps are bitwise equal."""
+    sizes = [64, 160, 96]
+    c0 = [np.random.default_rng(30 + k).uniform(-0.1, 0.1, (n, n)) for k, n in enumerate(sizes)]
+    ref = None
+    for cfg in range(CH_CONFIGS):
+        b = cs.CahnHilliardBatch(sizes)
+        b.set_config(cfg)
+        for k, c in enumerate(c0):
+            b.set_state(k, c)
+        b.step(6)
+        b.synchronize()
+        got = [b.state(k) for k in range(len(sizes))]
+        b.close()
+        if ref is None:
+            ref = got
+            continue
+        for (cur, old), (rcur, rold) in zip(got, ref):
+            assert cur.tobytes() == rcur.tobytes() and old.tobytes() == rold.tobytes(), cfg
+
+
+def test_batch_autotune_leaves_the_state_unchanged(gpu):
+    sizes = [128, 64]
+    c0 = [np.random.default_rng(40 + k).uniform(-0.1, 0.1, (n, n)) for k, n in enumerate(sizes)]
+    b = cs.CahnHilliardBatch(sizes)
+    for k, c in enumerate(c0):
+        b.set_state(k, c)
+    b.step(3)
+    b.synchronize()
+    before = [b.state(k) for k in range(len(sizes))]
+    name = b.autotune(steps=2)
+    assert name.startswith("rhs_warps") and b.config() == name
+    after = [b.state(k) for k in range(len(sizes))]
+    for (c1, o1), (c2, o2) in zip(before, after):
+        assert c1.tobytes() == c2.tobytes() and o1.tobytes() == o2.tobytes()
+    b.step(4)
+    b.synchronize()
+    ref = cs.CahnHilliardBatch(sizes)
+    for k, c in enumerate(c0):
+        ref.set_state(k, c)
+    ref.step(7)
+    ref.synchronize()
+    for k in range(len(sizes)):
+        assert b.state(k)[0].tobytes() == ref.state(k)[0].tobytes()
+    b.close()
+    ref.close()
