@@ -262,6 +262,25 @@ def reference_gpu(args) -> dict:
         oracle.reference_weno(n, n, 1, 32, 8, o.data_ptr(), f.data_ptr(), u.data_ptr(), vv.data_ptr(), 1 / h, 1 / h)
     dt = (time.perf_counter() - t0) / 3
     out["weno"] = {"gpts_s": round(n * n / dt / 1e9, 3), "config": f"{n}^2, BLOCK 32x8, u, v ~ U(-1, 1)"}
+    # cuPentBatch's kernels
+    if oracle.ReferenceCahnHilliardGPU.available():
+        pm, pb = 256, 1 << 18
+        base = pent_inputs(torch, dev, pm, pb)
+        work = [a.clone() for a in base[:5]]
+        copy_ms = event_ms(torch, lambda: [a.copy_(b) for a, b in zip(work, base[:5])])
+        f_ms = event_ms(torch, lambda: ([a.copy_(b) for a, b in zip(work, base[:5])],
+                                        oracle.reference_pent(True, [a.data_ptr() for a in work], pm, pb))) - copy_ms
+        bb = base[5].clone()
+        bcopy_ms = event_ms(torch, lambda: bb.copy_(base[5]))
+        s_ms = event_ms(torch, lambda: (bb.copy_(base[5]), oracle.reference_pent(
+            False, [a.data_ptr() for a in work] + [bb.data_ptr()], pm, pb))) - bcopy_ms
+        rows = pm * pb
+        out["pent_batch"] = {"factor_grows_s": round(rows / (f_ms * 1e-3) / 1e9, 2),
+                             "solve_grows_s": round(rows / (s_ms * 1e-3) / 1e9, 2),
+                             "config": f"{pb} systems x {pm} unknowns, 64-thread blocks (BLOCK_INV)",
+                             "method": "pentFactorBatch / pentSolveBatch, event time (each launch synchronised)"}
+        del base, work, bb
+        torch.cuda.empty_cache()
     del f, o, u, vv
     torch.cuda.empty_cache()
     # Cahn-Hilliard: the reference program, one grid at a time
@@ -487,6 +506,11 @@ def run_gpu(args, world, rank, local):
     if not args.skip_weno:
         weno = run_weno(cs, torch, dev, n, fp64_rate)
 
+    # ---- batched pentadiagonal systems (cuPentBatch) ----
+    pent = None
+    if not args.skip_pent:
+        pent = run_pent(cs, torch, dev, hbm_peak)
+
     # ---- e2e: reference-facing API with host buffers (numTiles=4, HOST offload) ----
     e2e = e2e_managed = None
     if not args.skip_e2e:
@@ -568,6 +592,8 @@ def run_gpu(args, world, rank, local):
             line["sizes"] = sizes_out
         if weno is not None:
             line["weno"] = weno
+        if pent is not None:
+            line["pent_batch"] = pent
         if cpu_ch is not None:
             line["cpu_baseline_ch"] = cpu_ch
         if ch_batched is not None:
@@ -702,6 +728,64 @@ def run_size_sweep(cs, torch, dev, local, sizes=(1024, 2048, 4096, 8192), tiles=
             del graph, outs, keep
         del inp
         torch.cuda.synchronize(dev)
+    return out
+
+
+def pent_inputs(torch, dev, m, batch):
+    """Diagonally dominant interleaved systems (seeded): ds, dl, d, du, dw, b of shape (m, batch)."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+
+    def r():
+        return torch.rand((m, batch), device=dev, dtype=torch.float64, generator=g) * 2 - 1
+    ds, dl, du, dw, b = r(), r(), r(), r(), r()
+    d = torch.rand((m, batch), device=dev, dtype=torch.float64, generator=g) * 3 + 5
+    ds[:2] = 0
+    dl[:1] = 0
+    du[m - 1:] = 0
+    dw[m - 2:] = 0
+    return [ds, dl, d, du, dw, b]
+
+
+def event_ms(torch, fn, reps=5):
+    fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return sorted(times)[len(times) // 2]
+
+
+def run_pent(cs, torch, dev, hbm_peak, m=256, batch=1 << 18):
+    """cuPentBatch's factorisation and solve over `batch` interleaved systems of m unknowns (the layout's
+    wire format), and the inverted-pivot solve; 72 B per row of compulsory traffic in each."""
+    base = pent_inputs(torch, dev, m, batch)
+    work = [a.clone() for a in base[:5]]
+    rows = m * batch
+    copy_ms = event_ms(torch, lambda: [a.copy_(b) for a, b in zip(work, base[:5])])
+    f_ms = event_ms(torch, lambda: ([a.copy_(b) for a, b in zip(work, base[:5])],
+                                    cs.pent_factor_batch(*work, m, batch))) - copy_ms
+    bb = base[5].clone()
+    bcopy_ms = event_ms(torch, lambda: bb.copy_(base[5]))
+    s_ms = event_ms(torch, lambda: (bb.copy_(base[5]), cs.pent_solve_batch(*work, bb, m, batch))) - bcopy_ms
+    rd = work[2].clone()
+    cs.pent_invert_pivots(rd, m, batch)
+    r_ms = event_ms(torch, lambda: (bb.copy_(base[5]), cs.pent_solve_batch(work[0], work[1], rd, work[3], work[4], bb,
+                                                                            m, batch, inverted_pivots=True))) - bcopy_ms
+    out = {"config": f"{batch} systems x {m} unknowns, interleaved [row * batch + system], FP64"}
+    for nm, ms in (("factor", f_ms), ("solve", s_ms), ("solve_inverted_pivots", r_ms)):
+        out[nm] = {"grows_s": round(rows / (ms * 1e-3) / 1e9, 2), "ms": round(ms, 4),
+                   "hbm_gbs": round(72.0 * rows / (ms * 1e-3) / 1e9, 1),
+                   "hbm_frac": round(72.0 * rows / (ms * 1e-3) / 1e9 / hbm_peak, 4)}
+    out["note"] = ("factor and exact solve: bit-identical to cuPentBatch, FP64-bound by their correctly rounded "
+                   "divisions; inverted pivots: HBM-bound")
+    del base, work, bb, rd
+    torch.cuda.empty_cache()
     return out
 
 
@@ -873,6 +957,7 @@ def main():
     ap.add_argument("--skip-sizes", action="store_true")
     ap.add_argument("--skip-weno", action="store_true")
     ap.add_argument("--skip-indirect", action="store_true")
+    ap.add_argument("--skip-pent", action="store_true")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],
                     help="kernel configuration choice: 0 defaults, 1 tune at the first Compute (default), 2 always")
     ap.add_argument("--traffic", type=float, default=None,

@@ -87,6 +87,13 @@ def lib() -> ctypes.CDLL:
         L.custen_set_device.argtypes = [i]
         L.custen_probe_fma_rate.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
         dp = ctypes.POINTER(ctypes.c_double)
+        L.custen_pent_last_error.restype = ctypes.c_char_p
+        for name in ("custen_pent_factor_batch",):
+            getattr(L, name).argtypes = [vp, vp, vp, vp, vp, i, i, vp]
+        for name in ("custen_pent_solve_batch", "custen_pent_solve_batch_rcp"):
+            getattr(L, name).argtypes = [vp, vp, vp, vp, vp, vp, i, i, vp]
+        L.custen_pent_invert_pivots.argtypes = [vp, i, i, vp]
+        L.custen_pent_set_depth.argtypes = [i, i]
         L.custen_ch_last_error.restype = ctypes.c_char_p
         L.custen_ch_batch_create.argtypes = [ctypes.POINTER(vp), i, ctypes.POINTER(i), dp, ctypes.c_double,
                                              ctypes.c_double, i, vp]
@@ -275,6 +282,33 @@ class WenoAdvection(Stencil):
         _check(lib().custen_create_2d_xyweno_adv_p(self.handle, device, num_tiles, nx, ny, block_x, block_y,
                                                    float(dx), float(dy), addr(u), addr(v), addr(out), addr(inp)))
         self._alive = True
+
+
+def _pent_check(status: int) -> None:
+    if status != 0:
+        raise CustenError(lib().custen_pent_last_error().decode())
+
+
+def pent_factor_batch(ds, dl, d, du, dw, m: int, batch: int, stream=None) -> None:
+    """cuPentBatch's pentFactorBatch in place on device arrays in the interleaved layout [i * batch + s]."""
+    _pent_check(lib().custen_pent_factor_batch(addr(ds), addr(dl), addr(d), addr(du), addr(dw), m, batch,
+                                               _stream_ptr(stream)))
+
+
+def pent_solve_batch(ds, dl, d, du, dw, b, m: int, batch: int, stream=None, inverted_pivots: bool = False) -> None:
+    """cuPentBatch's pentSolveBatch (b overwritten by x); inverted_pivots: d holds 1 / pivot."""
+    fn = lib().custen_pent_solve_batch_rcp if inverted_pivots else lib().custen_pent_solve_batch
+    _pent_check(fn(addr(ds), addr(dl), addr(d), addr(du), addr(dw), addr(b), m, batch, _stream_ptr(stream)))
+
+
+def pent_invert_pivots(d, m: int, batch: int, stream=None) -> None:
+    _pent_check(lib().custen_pent_invert_pivots(addr(d), m, batch, _stream_ptr(stream)))
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return stream if isinstance(stream, int) else int(getattr(stream, "cuda_stream", 0))
 
 
 class CuStenT(ctypes.Structure):

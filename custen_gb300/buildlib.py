@@ -38,7 +38,8 @@ CFG_UNITS = [(f"stencil_cfg_{d}_{k}", "stencil_cfg.cu", [f"-DCUSTEN_CFG_DTYPE={d
 LIB_UNITS = [("plan", "plan.cu", []), ("stencil_dispatch", "stencil_dispatch.cu", []), ("weno", "weno.cu", []),
              ("autotune", "autotune.cu", [])] + CFG_UNITS
 # Extra translation units of the shared library.
-SO_UNITS = [(Path(s).stem, s, []) for s in ("builtin_funs.cu", "probe.cu", "ch_solver.cu", "ch_server.cu")]
+SO_UNITS = [(Path(s).stem, s, []) for s in ("builtin_funs.cu", "probe.cu", "ch_solver.cu", "ch_server.cu",
+                                            "pent_batch.cu")]
 
 
 def nvcc() -> str:

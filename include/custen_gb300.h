@@ -161,6 +161,28 @@ int custen_probe_fma_rate(int dtype, double* fma_per_s);
  * No counterpart in the reference (its kernels have no waits). */
 int custen_device_error(unsigned int* flags, int clear);
 
+/* ---- batched pentadiagonal systems (cuPentBatch, cuPentCahnADI/src/cuPentBatch.cu) ----
+ * Interleaved layout: element (row i, system s) of each diagonal and of b at [i * batch + s]; ds, dl
+ * two / one below the main diagonal d, du, dw one / two above (ds[0..1], dl[0], du[m-1], dw[m-2..m-1]
+ * zero). Device pointers; asynchronous on `stream` (NULL: the default stream). m >= 4.
+ * custen_pent_factor_batch   -- pentFactorBatch (:35-113), in place, bit-identical to the reference kernel
+ * custen_pent_solve_batch    -- pentSolveBatch (:119-198) with those factors, b overwritten by x,
+ *                               bit-identical to the reference kernel
+ * custen_pent_invert_pivots  -- d <- 1 / d after the factorisation (no reference counterpart)
+ * custen_pent_solve_batch_rcp -- the solve with inverted pivots: multiplications instead of divisions,
+ *                               rounding within about one unit in the last place per row of the reference */
+int custen_pent_factor_batch(double* ds, double* dl, double* d, double* du, double* dw, int m, int batch,
+                             void* stream);
+int custen_pent_solve_batch(const double* ds, const double* dl, const double* d, const double* du, const double* dw,
+                            double* b, int m, int batch, void* stream);
+int custen_pent_invert_pivots(double* d, int m, int batch, void* stream);
+int custen_pent_solve_batch_rcp(const double* ds, const double* dl, const double* rd, const double* du,
+                                const double* dw, double* b, int m, int batch, void* stream);
+const char* custen_pent_last_error(void);
+/* Rows of loads issued ahead of the recurrence (2, 4 or 8) in the factorisation (which = 0), the exact
+ * solve (1) and the inverted-pivot solve (2); results do not depend on it. */
+int custen_pent_set_depth(int which, int rows);
+
 /* ---- Cahn-Hilliard ADI solver: batches of periodic grids of different sizes ----
  * The method of cuPentCahnADI (cuPentCahnADI/src/cuPentCahnADI.cu:197-627 with BatchHyper.cu and
  * cuPentBatch.cu): D = 1, gamma, dt = dt_factor * dx, domain [0, lx)^2, BDF2 / ADI with cyclic

@@ -5,6 +5,7 @@ baseline leg as the checker; never by the library).
   see the header of that file).
 * ``weno_oracle.c``: C restatement of the periodic WENO5 advection operator
   (cuSten/src/kernels/2d_xyADVWENO_p_kernel.cu).
+* ``pent_oracle.c``: C restatement of cuPentBatch's batched pentadiagonal factorisation and solve.
 * ``ch_oracle.c``: C restatement of the Cahn-Hilliard ADI solver of
   cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c.
 * ``ref_build.py``: builds the reference's own code from the reference sources into ``oracle/_ref``
@@ -23,7 +24,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "liboracle.so"
-SOURCES = [HERE / "stencil_oracle.c", HERE / "ch_oracle.c", HERE / "weno_oracle.c"]
+SOURCES = [HERE / "stencil_oracle.c", HERE / "ch_oracle.c", HERE / "weno_oracle.c", HERE / "pent_oracle.c"]
 HEADERS = [HERE / "stencil_oracle_impl.h"]
 
 REFRUN = BUILD / "librefrun.so"
@@ -99,6 +100,10 @@ def lib() -> ctypes.CDLL:
         L.oracle_host_loop_f64.argtypes = [i, i, vp, vp, vp, i, i, i, i, i, i, i]
         L.oracle_weno_f64.argtypes = [i, i, vp, vp, vp, vp, ctypes.c_double, ctypes.c_double]
         L.oracle_weno_f64.restype = None
+        L.oracle_pent_factor.argtypes = [vp, vp, vp, vp, vp, i, i]
+        L.oracle_pent_factor.restype = None
+        L.oracle_pent_solve.argtypes = [vp, vp, vp, vp, vp, vp, i, i]
+        L.oracle_pent_solve.restype = None
         L.ch_oracle_create.argtypes = [i, ctypes.c_double, vp]
         L.ch_oracle_create.restype = vp
         L.ch_oracle_step.argtypes = [vp, i]
@@ -140,6 +145,23 @@ def weno(inp: np.ndarray, u: np.ndarray, v: np.ndarray, cdx: float, cdy: float) 
     lib().oracle_weno_f64(nx, ny, inp.ctypes.data, u.ctypes.data, v.ctypes.data, out.ctypes.data, float(cdx),
                           float(cdy))
     return out
+
+
+def pent_factor(ds, dl, d, du, dw):
+    """cuPentBatch's pentFactorBatch on (m, batch) arrays in the interleaved layout; returns new arrays."""
+    arrs = [np.array(a, dtype=np.float64, order="C", copy=True) for a in (ds, dl, d, du, dw)]
+    m, batch = arrs[0].shape
+    lib().oracle_pent_factor(*[a.ctypes.data for a in arrs], m, batch)
+    return arrs
+
+
+def pent_solve(factors, b):
+    """cuPentBatch's pentSolveBatch with the factors of pent_factor; returns the solution."""
+    fs = [np.ascontiguousarray(a, dtype=np.float64) for a in factors]
+    x = np.array(b, dtype=np.float64, order="C", copy=True)
+    m, batch = x.shape
+    lib().oracle_pent_solve(*[a.ctypes.data for a in fs], x.ctypes.data, m, batch)
+    return x
 
 
 def host_loop_xyp(inp: np.ndarray, w: np.ndarray, H: int, L: int, V: int, T: int, y0: int = 0,
@@ -276,22 +298,28 @@ class ReferenceCahnHilliardGPU:
     def available() -> bool:
         return REF_CH_CUBIN.exists()
 
-    def __init__(self, c0: np.ndarray, lx: float = 2 * np.pi):
+    @staticmethod
+    def _load():
         global _refch
         if _refch is None:
             build()
             R = ctypes.CDLL(str(REFCH))
-            vp = ctypes.c_void_p
+            vp, i = ctypes.c_void_p, ctypes.c_int
             R.refch_error.restype = ctypes.c_char_p
             R.refch_load.argtypes = [ctypes.c_char_p]
-            R.refch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_double, vp, vp, vp, vp]
-            R.refch_step.argtypes = [vp, ctypes.c_int]
+            R.refch_create.argtypes = [ctypes.POINTER(vp), i, ctypes.c_double, vp, vp, vp, vp]
+            R.refch_step.argtypes = [vp, i]
             R.refch_get.argtypes = [vp, vp, vp]
             R.refch_destroy.argtypes = [vp]
+            R.refch_pent_factor.argtypes = [vp, vp, vp, vp, vp, i, i]
+            R.refch_pent_solve.argtypes = [vp, vp, vp, vp, vp, vp, i, i]
             if R.refch_load(str(REF_CH_CUBIN).encode()) != 0:
                 raise RuntimeError(R.refch_error().decode())
             _refch = R
-        self._R = _refch
+        return _refch
+
+    def __init__(self, c0: np.ndarray, lx: float = 2 * np.pi):
+        self._R = self._load()
         c0 = np.ascontiguousarray(c0, dtype=np.float64)
         n = c0.shape[0]
         self.n = n
@@ -319,3 +347,13 @@ class ReferenceCahnHilliardGPU:
         if self._h:
             self._R.refch_destroy(self._h)
             self._h = None
+
+
+def reference_pent(factor: bool, ptrs, m: int, batch: int) -> None:
+    """Run the reference's pentFactorBatch (ptrs: ds, dl, d, du, dw) or pentSolveBatch (ptrs: ds, dl, d,
+    du, dw, b) on device pointers (the reference CH cubin)."""
+    ReferenceCahnHilliardGPU._load()
+    R = _refch
+    rc = R.refch_pent_factor(*ptrs, m, batch) if factor else R.refch_pent_solve(*ptrs, m, batch)
+    if rc != 0:
+        raise RuntimeError(R.refch_error().decode())

@@ -300,6 +300,28 @@ int refch_get(void* st, double* c_curr, double* c_old) {
     return 0;
 }
 
+// The reference's batched pentadiagonal kernels on caller buffers (device pointers), launched as the
+// program launches them: 64-thread blocks over the systems (cuPentCahnADI.cu:357, BatchHyper.cu:565).
+int refch_pent_factor(double* ds, double* dl, double* d, double* du, double* dw, int m, int batch) {
+    if (!g_mod) {
+        snprintf(g_err, sizeof(g_err), "reference CH cubin not loaded");
+        return 1;
+    }
+    void* a[] = {&ds, &dl, &d, &du, &dw, &m, &batch};
+    if (launch(K_FACTOR, (unsigned)((batch + 63) / 64), 1, 64, 1, a)) return 1;
+    return sync("pentFactorBatch");
+}
+
+int refch_pent_solve(double* ds, double* dl, double* d, double* du, double* dw, double* b, int m, int batch) {
+    if (!g_mod) {
+        snprintf(g_err, sizeof(g_err), "reference CH cubin not loaded");
+        return 1;
+    }
+    void* a[] = {&ds, &dl, &d, &du, &dw, &b, &m, &batch};
+    if (launch(K_SOLVE, (unsigned)((batch + 63) / 64), 1, 64, 1, a)) return 1;
+    return sync("pentSolveBatch");
+}
+
 int refch_destroy(void* st) {
     State* s = static_cast<State*>(st);
     if (!s) return 0;

@@ -121,3 +121,29 @@ def weno_inputs(nx: int, ny: int, seed: int, rough: bool = False):
     v[rng.random((ny, nx)) < 0.05] = 0.0
     return (np.ascontiguousarray(f), np.ascontiguousarray(u), np.ascontiguousarray(v), 2 * np.pi / nx,
             2 * np.pi / ny)
+
+
+def pent_system(m: int, batch: int, seed: int):
+    """Diagonally dominant batched pentadiagonal systems in the interleaved layout (arrays of shape
+    (m, batch), element [i, s] = row i of system s): ds, dl, d, du, dw and a right-hand side b, with the
+    zero entries of cuPentBatch's convention (ds rows 0-1, dl row 0, du row m-1, dw rows m-2, m-1)."""
+    rng = np.random.default_rng(900 + seed)
+    ds, dl, du, dw = (rng.uniform(-1.0, 1.0, (m, batch)) for _ in range(4))
+    d = rng.uniform(5.0, 8.0, (m, batch)) * np.where(rng.random((m, batch)) < 0.5, 1.0, -1.0)
+    ds[:2] = 0.0
+    dl[:1] = 0.0
+    du[m - 1:] = 0.0
+    dw[m - 2:] = 0.0
+    b = rng.uniform(-1.0, 1.0, (m, batch))
+    return [np.ascontiguousarray(a) for a in (ds, dl, d, du, dw, b)]
+
+
+def pent_dense_apply(ds, dl, d, du, dw, x):
+    """A x for the unfactored systems (same layout), for residual checks."""
+    m = x.shape[0]
+    y = d * x
+    y[1:] += dl[1:] * x[:-1]
+    y[2:] += ds[2:] * x[:-2]
+    y[:-1] += du[:-1] * x[1:]
+    y[:-2] += dw[:-2] * x[2:]
+    return y
