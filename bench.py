@@ -367,6 +367,7 @@ def run_gpu(args, world, rank, local):
     cs.build()
     # Kernel configurations: tuned at each handle's first (warm-up) Compute and cached (autotune.cu)
     cs.set_tune_cache(str(ROOT / "_build" / f"tune_cache_rank{rank}.json"))
+    cs.set_stage_chunk_bytes(args.stage_chunk_mb << 20)
     cs.set_autotune(args.autotune)
     torch.cuda.set_device(local)
     cs._check(cs.lib().custen_set_device(local))
@@ -950,7 +951,7 @@ def main():
     ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--ch-sims", type=int, default=512)
     ap.add_argument("--ch-steps", type=int, default=500)
-    ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--served-requests", type=int, default=96)
     ap.add_argument("--served-rate", type=float, default=200.0)
     ap.add_argument("--served-chunk", type=int, default=16)
     ap.add_argument("--skip-ref-gpu", action="store_true")
@@ -958,6 +959,8 @@ def main():
     ap.add_argument("--skip-weno", action="store_true")
     ap.add_argument("--skip-indirect", action="store_true")
     ap.add_argument("--skip-pent", action="store_true")
+    ap.add_argument("--stage-chunk-mb", type=int, default=0,
+                    help="chunk size of the host-memory staging path (0: the library default)")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],
                     help="kernel configuration choice: 0 defaults, 1 tune at the first Compute (default), 2 always")
     ap.add_argument("--traffic", type=float, default=None,
