@@ -54,6 +54,13 @@ namespace ch {
 // level of one rounding per term, far inside the solver's 1e-10 parity bar.
 // NW warps per CTA share one 32 x 32 work item: shared memory limits residency to a few CTAs per SM, so
 // more warps per CTA give the FP64 pipe more warps to issue from (the tuned choice, ChConfig).
+//
+// The constant factors 2, -4 and -2/3 are read from device memory into registers once per thread: an
+// FP64 FMA that takes a literal or a kernel parameter as an operand issues about 19% slower on GB300
+// (507 against 602-628 G FMA/s measured) than one whose operands are all registers. The values, and
+// so the results, are the same as with literals.
+__device__ double g_rhs_factors[3] = {2.0, -4.0, -2.0 / 3.0};
+
 template <typename T, int NW>
 __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restrict__ grids,
                                                           const Item* __restrict__ items, int n_items, int parity,
@@ -65,6 +72,8 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
     constexpr int NT = NW * BLK;
     const int tid = threadIdx.x;
     const int lane = tid & (BLK - 1), warp = tid / BLK;
+    const volatile double* factors = g_rhs_factors;
+    const T two = (T)factors[0], m_four = (T)factors[1], m_two_thirds = (T)factors[2];
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
         __syncthreads();
@@ -94,7 +103,7 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
             const double cv = cur[(size_t)gy * n + gx];
             const double ov = old[(size_t)gy * n + gx];
             const T c32 = (T)cv, o32 = (T)ov;
-            cb[r][c] = fma((T)2, c32, -o32);
+            cb[r][c] = fma(two, c32, -o32);
             if (r >= 1 && r < 35 && c >= 1 && c < 35) hh[r - 1][c - 1] = s_nl * fma(c32 * c32, c32, -c32);
             if (r >= 2 && r < 34 && c >= 2 && c < 34) dco[r - 2][c - 2] = c32 - o32;
         }
@@ -103,7 +112,7 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
 #pragma unroll 4
         for (int e = tid; e < 34 * 34; e += NT) {
             const int r = e / 34, c = e - r * 34;
-            const T lap = fma((T)(-4), cb[r + 1][c + 1], (cb[r][c + 1] + cb[r + 2][c + 1]) + (cb[r + 1][c] + cb[r + 1][c + 2]));
+            const T lap = fma(m_four, cb[r + 1][c + 1], (cb[r][c + 1] + cb[r + 2][c + 1]) + (cb[r + 1][c] + cb[r + 1][c + 2]));
             hh[r][c] = fma(-s_lin, lap, hh[r][c]);
         }
         __syncthreads();
@@ -112,8 +121,8 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
         double* out = gd.tmp + (size_t)y0 * n + x0 + j;
 #pragma unroll 4
         for (int rr = warp; rr < BLK; rr += NW) {
-            const T lap = fma((T)(-4), hh[rr + 1][j + 1], (hh[rr][j + 1] + hh[rr + 2][j + 1]) + (hh[rr + 1][j] + hh[rr + 1][j + 2]));
-            out[(size_t)rr * n] = (double)fma((T)(-2.0 / 3.0), dco[rr][j], lap);
+            const T lap = fma(m_four, hh[rr + 1][j + 1], (hh[rr][j + 1] + hh[rr + 2][j + 1]) + (hh[rr + 1][j] + hh[rr + 1][j + 2]));
+            out[(size_t)rr * n] = (double)fma(m_two_thirds, dco[rr][j], lap);
         }
         __syncthreads();
     }

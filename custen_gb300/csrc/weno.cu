@@ -31,26 +31,45 @@ constexpr int kWenoDYH = kWenoTH + 5;       // y differences at rows y0-2 .. y0+
 constexpr size_t kWenoSmem = sizeof(double) * ((size_t)kWenoSH * kWenoSW + (size_t)kWenoTH * kWenoDXW +
                                                (size_t)kWenoDYH * kWenoTW);
 
+// Coefficients of the reconstruction. They are read from device memory into registers once per
+// thread (WenoCoeffs::load): an FP64 FMA or add with a literal or kernel-parameter operand issues about
+// 19% slower on GB300 than one whose operands are all registers (507 against 602-628 G FMA/s
+// measured). The values are the literals of the reference's expressions, so every result is the same.
+__device__ double g_weno_coeffs[15] = {1.0 / 3.0, 7.0 / 6.0, 11.0 / 6.0, 1.0 / 6.0, 5.0 / 6.0,
+                                       2.0,       4.0,       3.0,        13.0 / 12.0, 0.25,
+                                       1e-06,     0.1,       0.6,        0.3,         0.0};
+
+struct WenoCoeffs {
+    double third, seven_sixths, eleven_sixths, sixth, five_sixths, two, four, three, thirteen_twelfths,
+        quarter, eps, g1, g2, g3;
+    __device__ __forceinline__ void load() {
+        const volatile double* k = g_weno_coeffs;
+        third = k[0]; seven_sixths = k[1]; eleven_sixths = k[2]; sixth = k[3]; five_sixths = k[4];
+        two = k[5]; four = k[6]; three = k[7]; thirteen_twelfths = k[8]; quarter = k[9];
+        eps = k[10]; g1 = k[11]; g2 = k[12]; g3 = k[13];
+    }
+};
+
 // Fifth-order WENO reconstruction (Jiang & Shu 1996, in the notation of Osher & Fedkiw, "Level Set
 // Methods and Dynamic Implicit Surfaces", 3.4) from five consecutive differences a..e. The three
 // candidate stencils, the smoothness indicators and the nonlinear weights are evaluated in the order
 // of the reference's wenoSten (2d_xyADVWENO_p_kernel.cu:52-88): same expressions, same contraction,
 // and the smoothness squares and the squared (indicator + 1e-6) taken by powf in single precision.
-__device__ __forceinline__ double weno5(double a, double b, double c, double d, double e) {
-    const double q1 = (1.0 / 3.0) * a - (7.0 / 6.0) * b + (11.0 / 6.0) * c;
-    const double q2 = -(1.0 / 6.0) * b + (5.0 / 6.0) * c + (1.0 / 3.0) * d;
-    const double q3 = (1.0 / 3.0) * c + (5.0 / 6.0) * d - (1.0 / 6.0) * e;
+__device__ __forceinline__ double weno5(const WenoCoeffs& k, double a, double b, double c, double d, double e) {
+    const double q1 = k.third * a - k.seven_sixths * b + k.eleven_sixths * c;
+    const double q2 = -k.sixth * b + k.five_sixths * c + k.third * d;
+    const double q3 = k.third * c + k.five_sixths * d - k.sixth * e;
 
-    const double is1 = (13.0 / 12.0) * powf((float)(a - 2.0 * b + c), 2.0f) +
-                       0.25 * powf((float)(a - 4.0 * b + 3.0 * c), 2.0f);
-    const double is2 = (13.0 / 12.0) * powf((float)(b - 2.0 * c + d), 2.0f) + 0.25 * powf((float)(b - d), 2.0f);
-    const double is3 = (13.0 / 12.0) * powf((float)(c - 2.0 * d + e), 2.0f) +
-                       0.25 * powf((float)(3.0 * c - 4.0 * d + e), 2.0f);
+    const double is1 = k.thirteen_twelfths * powf((float)(a - k.two * b + c), 2.0f) +
+                       k.quarter * powf((float)(a - k.four * b + k.three * c), 2.0f);
+    const double is2 = k.thirteen_twelfths * powf((float)(b - k.two * c + d), 2.0f) +
+                       k.quarter * powf((float)(b - d), 2.0f);
+    const double is3 = k.thirteen_twelfths * powf((float)(c - k.two * d + e), 2.0f) +
+                       k.quarter * powf((float)(k.three * c - k.four * d + e), 2.0f);
 
-    const double eps = 1e-06;
-    const double g1 = 0.1 / powf((float)(is1 + eps), 2.0f);
-    const double g2 = 0.6 / powf((float)(is2 + eps), 2.0f);
-    const double g3 = 0.3 / powf((float)(is3 + eps), 2.0f);
+    const double g1 = k.g1 / powf((float)(is1 + k.eps), 2.0f);
+    const double g2 = k.g2 / powf((float)(is2 + k.eps), 2.0f);
+    const double g3 = k.g3 / powf((float)(is3 + k.eps), 2.0f);
     const double norm = 1.0 / (g1 + g2 + g3);
     const double w1 = g1 * norm, w2 = g2 * norm, w3 = g3 * norm;
     return q1 * w1 + q2 * w2 + q3 * w3;
@@ -105,6 +124,8 @@ __global__ void __launch_bounds__(kWenoThreads, 2) weno_adv_kernel(double* __res
     const int tx = tid % kWenoTW;
     const int x = x0 + tx;
     if (x >= nx) return;
+    WenoCoeffs k;
+    k.load();
     for (int ty = tid / kWenoTW; ty < kWenoTH; ty += kWenoThreads / kWenoTW) {
         const int y = y0 + ty;
         if (y >= rows) break;
@@ -114,11 +135,11 @@ __global__ void __launch_bounds__(kWenoThreads, 2) weno_adv_kernel(double* __res
         // conditional expression would let the compiler evaluate both and double the FP64 work).
         const double* dr = dxs + ty * kWenoDXW + tx;      // dr[k] = D at column x - 2 + k
         const bool ux = uu > 0.0;
-        const double fx = weno5(ux ? dr[0] : dr[5], ux ? dr[1] : dr[4], dr[2 + !ux], ux ? dr[3] : dr[2],
+        const double fx = weno5(k, ux ? dr[0] : dr[5], ux ? dr[1] : dr[4], dr[2 + !ux], ux ? dr[3] : dr[2],
                                 ux ? dr[4] : dr[1]);
         const double* dc = dys + ty * kWenoTW + tx;       // dc[k * TW] = D at row y - 2 + k
         const bool vy = vv > 0.0;
-        const double fy = weno5(vy ? dc[0] : dc[5 * kWenoTW], vy ? dc[kWenoTW] : dc[4 * kWenoTW],
+        const double fy = weno5(k, vy ? dc[0] : dc[5 * kWenoTW], vy ? dc[kWenoTW] : dc[4 * kWenoTW],
                                 dc[(2 + !vy) * kWenoTW], vy ? dc[3 * kWenoTW] : dc[2 * kWenoTW],
                                 vy ? dc[4 * kWenoTW] : dc[kWenoTW]);
         // (2d_xyADVWENO_p_kernel.cu:424)
