@@ -510,7 +510,7 @@ def run_gpu(args, world, rank, local):
     # ---- batched pentadiagonal systems (cuPentBatch) ----
     pent = None
     if not args.skip_pent:
-        pent = run_pent(cs, torch, dev, hbm_peak)
+        pent = run_pent(cs, torch, dev, hbm_peak, batch=args.pent_batch)
 
     # ---- e2e: reference-facing API with host buffers (numTiles=4, HOST offload) ----
     e2e = e2e_managed = None
@@ -959,6 +959,7 @@ def main():
     ap.add_argument("--skip-weno", action="store_true")
     ap.add_argument("--skip-indirect", action="store_true")
     ap.add_argument("--skip-pent", action="store_true")
+    ap.add_argument("--pent-batch", type=int, default=1 << 18, help="systems in the pentadiagonal leg (256 unknowns each)")
     ap.add_argument("--stage-chunk-mb", type=int, default=0,
                     help="chunk size of the host-memory staging path (0: the library default)")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],

@@ -108,6 +108,13 @@ def lib() -> ctypes.CDLL:
         L.custen_ch_batch_autotune.argtypes = [vp, i, ctypes.c_char_p, sz]
         L.custen_ch_batch_config.argtypes = [vp, ctypes.c_char_p, sz]
         L.custen_ch_batch_set_config.argtypes = [vp, i]
+        L.custen_ch_batch_save.argtypes = [vp, i, ctypes.c_char_p, ctypes.c_double]
+        L.custen_ch_batch_load.argtypes = [vp, i, ctypes.c_char_p, dp]
+        L.custen_h5_write.argtypes = [ctypes.c_char_p, i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(vp),
+                                      ctypes.POINTER(ctypes.c_longlong)]
+        L.custen_h5_read.argtypes = [ctypes.c_char_p, ctypes.c_char_p, vp, ctypes.c_longlong,
+                                     ctypes.POINTER(ctypes.c_longlong)]
+        L.custen_h5_last_error.restype = ctypes.c_char_p
         L.custen_ch_server_last_error.restype = ctypes.c_char_p
         L.custen_ch_server_create.argtypes = [ctypes.POINTER(vp), ctypes.c_double, i, ctypes.c_double, ctypes.c_double,
                                               i, i]
@@ -352,6 +359,40 @@ def _ch_check(status: int) -> None:
         raise CustenError(lib().custen_ch_last_error().decode(errors="replace"))
 
 
+def snapshot_name(time: float) -> str:
+    """File name of the reference solver's snapshot at `time` (cuPentCahnADI.cu:107-110)."""
+    return "cahn_hilliard_%0.10f.nc" % time
+
+
+def h5_write(path, datasets) -> None:
+    """Write an HDF5 file whose root group holds the given two-dimensional float64 datasets
+    ({name: array}, 1 to 8 of them), in the format of the reference solver's snapshots."""
+    import numpy as np
+    items = [(str(k), np.ascontiguousarray(v, dtype=np.float64)) for k, v in dict(datasets).items()]
+    arrays = [a.reshape(a.shape if a.ndim == 2 else (a.size, 1) if a.ndim == 1 else (1, 1)) for _, a in items]
+    if any(a.ndim != 2 for a in arrays):
+        raise CustenError("h5_write: datasets must have rank 0, 1 or 2")
+    names = (ctypes.c_char_p * len(items))(*[k.encode() for k, _ in items])
+    ptrs = (ctypes.c_void_p * len(items))(*[a.ctypes.data for a in arrays])
+    dims = (ctypes.c_longlong * (2 * len(items)))(*[d for a in arrays for d in a.shape])
+    if lib().custen_h5_write(os.fsencode(path), len(items), names, ptrs, dims) != 0:
+        raise CustenError(lib().custen_h5_last_error().decode(errors="replace"))
+
+
+def h5_read(path, name: str):
+    """Read one float dataset of an HDF5 file (version-0/1 superblock, contiguous storage) as a
+    two-dimensional float64 array."""
+    import numpy as np
+    dims = (ctypes.c_longlong * 2)()
+    L = lib()
+    if L.custen_h5_read(os.fsencode(path), name.encode(), None, 0, dims) != 0:
+        raise CustenError(L.custen_h5_last_error().decode(errors="replace"))
+    out = np.empty((dims[0], dims[1]))
+    if L.custen_h5_read(os.fsencode(path), name.encode(), out.ctypes.data, out.size, dims) != 0:
+        raise CustenError(L.custen_h5_last_error().decode(errors="replace"))
+    return out
+
+
 class CahnHilliardBatch:
     """Many periodic Cahn-Hilliard ADI simulations of different sizes advanced together on the GPU
     (the solver of cuPentCahnADI, batched; include/custen_gb300.h)."""
@@ -404,6 +445,17 @@ class CahnHilliardBatch:
     def set_config(self, index: int) -> None:
         """Pin the kernel configuration (0 .. 5; -1: the default)."""
         _ch_check(lib().custen_ch_batch_set_config(self.h, int(index)))
+
+    def save(self, sim: int, path, time: float = 0.0) -> None:
+        """Write grid `sim` to an HDF5 snapshot: "c" (cCurr, the reference's dataset), "c_old", "t"."""
+        _ch_check(lib().custen_ch_batch_save(self.h, sim, os.fsencode(path), float(time)))
+
+    def load(self, sim: int, path) -> float:
+        """Resume grid `sim` from an HDF5 snapshot (this library's or the reference's); returns its time
+        (NaN when the file has none)."""
+        t = ctypes.c_double()
+        _ch_check(lib().custen_ch_batch_load(self.h, sim, os.fsencode(path), ctypes.byref(t)))
+        return float(t.value)
 
     def synchronize(self) -> None:
         _ch_check(lib().custen_ch_batch_synchronize(self.h))

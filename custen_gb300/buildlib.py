@@ -39,7 +39,7 @@ LIB_UNITS = [("plan", "plan.cu", []), ("stencil_dispatch", "stencil_dispatch.cu"
              ("autotune", "autotune.cu", [])] + CFG_UNITS
 # Extra translation units of the shared library.
 SO_UNITS = [(Path(s).stem, s, []) for s in ("builtin_funs.cu", "probe.cu", "ch_solver.cu", "ch_server.cu",
-                                            "pent_batch.cu")]
+                                            "pent_batch.cu", "h5snap.cpp")]
 
 
 def nvcc() -> str:

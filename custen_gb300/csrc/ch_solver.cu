@@ -737,6 +737,51 @@ int custen_ch_batch_get_state(void* h, int sim, double* c_cur, double* c_old) {
     return 0;
 }
 
+// Snapshot of one grid in the reference's HDF5 format (Print_Out, cuPentCahnADI.cu:103-140): dataset
+// "c" = cCurr (n x n doubles), plus "c_old" = cOld and "t" = the time (1 x 1), which a resume needs
+// and a reader of the reference's files ignores.
+int custen_ch_batch_save(void* h, int sim, const char* path, double time) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || sim < 0 || sim >= (int)b->n.size() || !path) return ch_fail_arg("invalid arguments");
+    const long long n = b->n[sim];
+    std::vector<double> cur((size_t)(n * n)), old((size_t)(n * n));
+    const int rc = custen_ch_batch_get_state(h, sim, cur.data(), old.data());
+    if (rc) return rc;
+    const char* names[3] = {"c", "c_old", "t"};
+    const double* data[3] = {cur.data(), old.data(), &time};
+    const long long dims[6] = {n, n, n, n, 1, 1};
+    if (custen_h5_write(path, 3, names, data, dims)) return ch_fail_arg(std::string("Writing the snapshot: ") + custen_h5_last_error());
+    return 0;
+}
+
+// Resume one grid from a snapshot: "c" (required, n x n) becomes cCurr; cOld is "c_old" when present,
+// else cCurr too, as the reference starts from its initial condition (cuPentCahnADI.cu:295-305).
+// *time receives "t", or NaN when the file has none (the reference's own snapshots).
+int custen_ch_batch_load(void* h, int sim, const char* path, double* time) {
+    Batch* b = static_cast<Batch*>(h);
+    if (!b || sim < 0 || sim >= (int)b->n.size() || !path) return ch_fail_arg("invalid arguments");
+    const long long n = b->n[sim];
+    long long dims[2] = {0, 0};
+    if (custen_h5_read(path, "c", nullptr, 0, dims)) return ch_fail_arg(std::string("Reading the snapshot: ") + custen_h5_last_error());
+    if (dims[0] != n || dims[1] != n)
+        return ch_fail_arg("snapshot grid is " + std::to_string(dims[0]) + " x " + std::to_string(dims[1]) +
+                           ", grid " + std::to_string(sim) + " is " + std::to_string(n) + " x " + std::to_string(n));
+    std::vector<double> cur((size_t)(n * n)), old;
+    if (custen_h5_read(path, "c", cur.data(), n * n, dims)) return ch_fail_arg(std::string("Reading the snapshot: ") + custen_h5_last_error());
+    long long od[2] = {0, 0};
+    if (custen_h5_read(path, "c_old", nullptr, 0, od) == 0) {
+        if (od[0] != n || od[1] != n) return ch_fail_arg("snapshot c_old does not match c");
+        old.resize((size_t)(n * n));
+        if (custen_h5_read(path, "c_old", old.data(), n * n, od))
+            return ch_fail_arg(std::string("Reading the snapshot: ") + custen_h5_last_error());
+    }
+    double t = std::nan("");
+    long long td[2];
+    if (custen_h5_read(path, "t", nullptr, 0, td) == 0 && td[0] * td[1] == 1) custen_h5_read(path, "t", &t, 1, td);
+    if (time) *time = t;
+    return custen_ch_batch_set_state(h, sim, cur.data(), old.empty() ? nullptr : old.data());
+}
+
 // Advance every grid by `steps` steps; asynchronous on the batch's stream (graph replays for pairs of
 // steps, plain launches for an odd remainder) unless use_graph == 0.
 int custen_ch_batch_step(void* h, int steps, int use_graph) {

@@ -204,7 +204,26 @@ unsigned long long custen_ch_batch_launches(void* batch);
 int custen_ch_batch_autotune(void* batch, int steps, char* name, size_t len);
 int custen_ch_batch_config(void* batch, char* name, size_t len);
 int custen_ch_batch_set_config(void* batch, int index);   /* 0 .. 5; -1: the default */
+/* Checkpoint / resume of one grid through an HDF5 snapshot (the format below): save writes "c" = cCurr,
+ * "c_old" = cOld and "t" = time; load takes "c" (must be n x n), "c_old" if present (else cCurr, as the
+ * reference starts) and returns "t" in *time (NaN when absent, as in the reference's own snapshots).
+ * A resumed grid continues bit for bit as if never stopped. */
+int custen_ch_batch_save(void* batch, int sim, const char* path, double time);
+int custen_ch_batch_load(void* batch, int sim, const char* path, double* time);
 int custen_ch_batch_destroy(void* batch);
+
+/* ---- HDF5 snapshot files (host only; no HDF5 library needed) ----
+ * The file the reference solver writes (Print_Out, cuPentCahnADI/src/cuPentCahnADI.cu:103-140): an
+ * HDF5 file (superblock version 0, as the HDF5 library writes with default properties) whose root group
+ * holds two-dimensional datasets of IEEE little-endian doubles in contiguous storage; the reference's
+ * file holds one, "c", with dims {nx, ny}. custen_h5_write writes 1 to 8 datasets (dims[2i], dims[2i+1]
+ * of dataset i; names without '/'). custen_h5_read reads one dataset of such a file, or of any HDF5
+ * file with version-0/1 superblock, old-style groups and contiguous float32/float64 data; it stores
+ * the dims (rank 1 gives {d0, 1}) and, when out is not NULL, the values (capacity in doubles). */
+int custen_h5_write(const char* path, int count, const char* const* names, const double* const* data,
+                    const long long* dims);
+int custen_h5_read(const char* path, const char* name, double* out, long long capacity, long long* dims);
+const char* custen_h5_last_error(void);
 
 /* ---- Cahn-Hilliard serving: request loop with continuous batching ----
  * Requests (n, steps, c0 or a seed for c0 ~ U(-0.1, 0.1), arrival time) are queued, then run()
