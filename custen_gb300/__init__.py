@@ -17,7 +17,9 @@ import os
 from pathlib import Path
 
 _PKG = Path(__file__).resolve().parent
-LIB_PATH = _PKG / "libcusten_gb300.so"
+# CUSTEN_CHECKED=1 selects the checked build (index checks that raise device error bit 1 instead of
+# faulting; build(checked=True)).
+LIB_PATH = _PKG / ("libcusten_gb300_checked.so" if os.environ.get("CUSTEN_CHECKED") == "1" else "libcusten_gb300.so")
 
 # Variant codes (include/custen_gb300.h).
 XP, XNP, XPFUN, XNPFUN, YP, YNP, YPFUN, YNPFUN, XYP, XYNP, XYPFUN, XYNPFUN = range(12)
@@ -36,9 +38,9 @@ class CustenError(RuntimeError):
     pass
 
 
-def build() -> Path:
+def build(checked: bool = False) -> Path:
     from . import buildlib
-    return buildlib.build()
+    return buildlib.build(checked=checked)
 
 
 def lib() -> ctypes.CDLL:
@@ -124,6 +126,8 @@ def lib() -> ctypes.CDLL:
         L.custen_ch_server_stats.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), dp, ctypes.POINTER(i), dp,
                                              ctypes.POINTER(ull)]
         L.custen_ch_server_destroy.argtypes = [vp]
+        L.custen_ch_server_request_state.argtypes = [vp, i, ctypes.POINTER(i)]
+        L.custen_ch_server_inject_failure.argtypes = [vp, i, i]
         L.custen_ch_step_noalloc.argtypes = [vp, vp, vp, i, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
         _lib = L
     return _lib
@@ -206,9 +210,20 @@ def set_stage_chunk_bytes(nbytes: int) -> None:
 
 
 def device_error(clear: bool = True) -> int:
-    """Device-side error flags (bit 0: a bounded mbarrier wait expired)."""
+    """Device-side error flags (bit 0: a bounded mbarrier wait expired; bit 1, checked builds only: an
+    index outside its extent, the access skipped)."""
     f = ctypes.c_uint()
     _check(lib().custen_device_error(ctypes.byref(f), int(clear)))
+    return int(f.value)
+
+
+def selftest_wait_expiry(rounds: int = 1 << 12) -> int:
+    """Run the bounded-wait self-test (a wait nothing completes, `rounds` try_wait rounds); returns the
+    device error flags seen afterwards (bit 0 expected, left set)."""
+    f = ctypes.c_uint()
+    st = lib().custen_selftest_wait_expiry(ctypes.c_longlong(rounds), ctypes.byref(f))
+    if st != 0:
+        raise CustenError(f"wait-expiry self-test failed to run (status {st})")
     return int(f.value)
 
 
@@ -443,7 +458,7 @@ class CahnHilliardBatch:
         return buf.value.decode()
 
     def set_config(self, index: int) -> None:
-        """Pin the kernel configuration (0 .. 5; -1: the default)."""
+        """Pin the kernel configuration (0 .. 9; -1: the default)."""
         _ch_check(lib().custen_ch_batch_set_config(self.h, int(index)))
 
     def save(self, sim: int, path, time: float = 0.0) -> None:
@@ -520,6 +535,16 @@ class CahnHilliardServer:
         arrival, admit, done, m0, m1 = (v.value for v in vals)
         return {"field": out, "arrival": arrival, "admit": admit, "done": done, "mean0": m0, "mean_end": m1,
                 "ttc": done - arrival}
+
+    def state(self, rid: int) -> str:
+        """"pending", "resident", "done" or "failed" (result() then raises with the reason)."""
+        st = ctypes.c_int()
+        _srv_check(lib().custen_ch_server_request_state(self.h, rid, ctypes.byref(st)))
+        return ("pending", "resident", "done", "failed")[st.value]
+
+    def inject_failure(self, rid: int, kind: int = 1) -> None:
+        """Test hook: make the request's admission allocation fail (kind 1), on the host."""
+        _srv_check(lib().custen_ch_server_inject_failure(self.h, rid, kind))
 
     def stats(self):
         mk, pts, bts = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -5,6 +5,9 @@ Outputs (in-tree, git-ignored):
                                       (include/cuSten.h), kernels and the shipped Fun device functions.
   custen_gb300/libcuSten.a         -- static drop-in for the reference's libcuSten.a (relocatable device
                                       code; link the user program with nvcc -rdc=true, as with the reference).
+  custen_gb300/libcusten_gb300_checked.so -- build(checked=True) only: the shared library compiled with
+                                      -DCUSTEN_CHECKED=1 (index checks that raise a device error flag instead
+                                      of faulting, csrc/checked.cuh); loaded when CUSTEN_CHECKED=1.
 
 Every translation unit is compiled for sm_103a only, with relocatable device code so that the Fun
 variants can call device functions defined in other translation units.
@@ -24,6 +27,8 @@ CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "custen_gb300"
 SO_PATH = PKG / "libcusten_gb300.so"
 A_PATH = PKG / "libcuSten.a"
+CHECKED_BUILD = ROOT / "_build" / "custen_gb300_checked"
+CHECKED_SO_PATH = PKG / "libcusten_gb300_checked.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -39,7 +44,7 @@ LIB_UNITS = [("plan", "plan.cu", []), ("stencil_dispatch", "stencil_dispatch.cu"
              ("autotune", "autotune.cu", [])] + CFG_UNITS
 # Extra translation units of the shared library.
 SO_UNITS = [(Path(s).stem, s, []) for s in ("builtin_funs.cu", "probe.cu", "ch_solver.cu", "ch_server.cu",
-                                            "pent_batch.cu", "h5snap.cpp")]
+                                            "pent_batch.cu", "h5snap.cpp", "selftest.cu")]
 
 
 def nvcc() -> str:
@@ -66,18 +71,21 @@ def _headers() -> list[Path]:
     return sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> Path:
-    BUILD.mkdir(parents=True, exist_ok=True)
+def build(verbose: bool = False, jobs: int | None = None, checked: bool = False) -> Path:
+    build_dir = CHECKED_BUILD if checked else BUILD
+    so_path = CHECKED_SO_PATH if checked else SO_PATH
+    build_dir.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
     units = LIB_UNITS + SO_UNITS
-    objs = {name: BUILD / (name + ".o") for name, _, _ in units}
+    objs = {name: build_dir / (name + ".o") for name, _, _ in units}
+    defs = ["-DCUSTEN_CHECKED=1"] if checked else []
 
     def compile_one(unit) -> None:
         name, src, extra = unit
         out = objs[name]
         if _needs(out, [CSRC / src] + hdrs):
-            cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(CSRC / src), "-o", str(out)]
+            cmd = [cc, *ARCH, *NVCC_FLAGS, *defs, *extra, "-c", str(CSRC / src), "-o", str(out)]
             if verbose:
                 print(" ".join(cmd), flush=True)
             _run(cmd)
@@ -86,11 +94,13 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         list(ex.map(compile_one, units))
 
     all_objs = [str(objs[name]) for name, _, _ in units]
-    if _needs(SO_PATH, list(objs.values())):
-        tmp = SO_PATH.with_suffix(".so.tmp")
+    if _needs(so_path, list(objs.values())):
+        tmp = so_path.with_suffix(".so.tmp")
         _run([cc, *ARCH, "-shared", "-rdc=true", "-Xcompiler", "-fPIC", *all_objs, "-o", str(tmp), "-cudart",
               "static"])
-        os.replace(tmp, SO_PATH)
+        os.replace(tmp, so_path)
+    if checked:
+        return so_path
     lib_objs = [objs[name] for name, _, _ in LIB_UNITS]
     if _needs(A_PATH, lib_objs):
         tmp = A_PATH.with_suffix(".a.tmp")

@@ -38,14 +38,17 @@ __global__ void ch_xsolve_kernel(const GridDev* __restrict__ grids, const Item* 
                                  unsigned int* counter);
 __global__ void ch_mass_kernel(const double* __restrict__ f, long long count, double* out);
 
-// Kernel configuration of a step: warps per right-hand-side CTA (1, 2, 4) and rows per batch of the y
-// sweep (16, 32). Every configuration computes the same values; the batch tuner times them.
+// Kernel configuration of a step: warps per right-hand-side CTA (1, 2, 4), rows per batch of the y
+// sweep (16, 32; with pipelined sweeps also the x sweep's columns per chunk), and whether the sweeps
+// copy the next chunk into shared memory while the current one runs. Every configuration computes the
+// same values; the batch tuner times them.
 struct ChConfig {
     int rhs_warps;
     int y_chunk;
+    int pipe;
 };
-constexpr ChConfig kChDefault{4, 16};
-constexpr int kChConfigs = 6;
+constexpr ChConfig kChDefault{4, 16, 0};
+constexpr int kChConfigs = 10;
 ChConfig ch_config(int index);   // 0 .. kChConfigs-1
 
 // One step of every grid of a work list: right-hand side, x sweep, y sweep (3 launches on s).

@@ -13,6 +13,7 @@
 // The solver is the reference's (cuPentCahnADI/src/cuPentCahnADI.cu:197-627); the request loop has
 // no counterpart in the reference, whose driver runs one simulation per process.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>   // header-only; the ranges cost nothing unless a profiler is attached
 
 #include <algorithm>
 #include <chrono>
@@ -50,7 +51,9 @@ struct Request {
     double arrival = 0.0;            // seconds on the server clock
     std::vector<double> c0;          // host initial field (empty: generated on the device from seed)
     unsigned long long seed = 0;
-    int state = 0;                   // 0 pending, 1 resident, 2 done
+    int state = 0;                   // 0 pending, 1 resident, 2 done, 3 failed (see error)
+    int inject = 0;                  // test hook: 1 = the device allocation at admission fails
+    std::string error;
     int remaining = 0;
     double admit_t = -1.0, done_t = -1.0;
     double mean0 = 0.0, mean_end = 0.0;
@@ -94,6 +97,7 @@ struct Server {
     int max_active = 0;
     double max_used = 0.0;
     unsigned long long launches = 0;
+    int failed = 0;
 };
 
 static thread_local std::string g_srv_err;
@@ -152,43 +156,87 @@ static int rebuild(Server* S) {
     return 0;
 }
 
+// Admission of one request. Returns 0 when it is resident, kAdmitFailed when it failed on its own
+// (an allocation or upload error: its partial allocations are released, the error is recorded in the
+// request, and the server keeps serving the others), or a fatal status when the device context itself
+// reports an error.
+constexpr int kAdmitFailed = -1;
+
 static int admit(Server* S, int id, double now) {
     Request& r = S->reqs[id];
+    nvtxRangePushA("admit");
     char key[128];
     snprintf(key, sizeof(key), "%d/%.17g", r.n, r.lx);
     r.table_key = key;
     TableRef& t = S->tables[key];
+    cudaError_t e = cudaSuccess;
+    const char* what = "";
+    auto step = [&](cudaError_t x, const char* w) {
+        if (e == cudaSuccess && x != cudaSuccess) {
+            e = x;
+            what = w;
+        }
+    };
+    // a fake of the failing allocation call, for tests of failure isolation: nothing is allocated
+    auto alloc = [&](double** p, size_t bytes) {
+        return r.inject == 1 ? cudaErrorMemoryAllocation : cudaMallocAsync(p, bytes, S->stream);
+    };
+    bool new_table = false;
     if (!t.ptr) {
         std::vector<double> h = build_table(r.n, r.lx, S->gamma, S->dt_factor);
         t.bytes = h.size() * sizeof(double);
-        SRV_TRY(cudaMallocAsync(&t.ptr, t.bytes, S->stream), "Allocating a solver table");
-        SRV_TRY(cudaMemcpyAsync(t.ptr, h.data(), t.bytes, cudaMemcpyHostToDevice, S->stream), "Uploading a table");
-        S->used += (double)t.bytes;
+        step(alloc(&t.ptr, t.bytes), "Allocating a solver table");
+        if (e == cudaSuccess) {
+            new_table = true;
+            // pageable source: the call returns once the vector has been read
+            step(cudaMemcpyAsync(t.ptr, h.data(), t.bytes, cudaMemcpyHostToDevice, S->stream), "Uploading a table");
+        }
     }
-    ++t.refs;
     const size_t f = (size_t)r.n * r.n * sizeof(double);
-    double* p[4];
-    for (int k = 0; k < 4; ++k)
-        SRV_TRY(cudaMallocAsync(&p[k], k < 3 ? f : 2 * (size_t)r.n * sizeof(double), S->stream), "Allocating a grid");
+    double* p[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        step(alloc(&p[k], k < 3 ? f : 2 * (size_t)r.n * sizeof(double)), "Allocating a grid");
+    double m = 0.0;
+    if (e == cudaSuccess) {
+        if (!r.c0.empty()) {
+            step(cudaMemcpyAsync(p[0], r.c0.data(), f, cudaMemcpyHostToDevice, S->stream), "Uploading c0");
+        } else {
+            const long long count = (long long)r.n * r.n;
+            ch_fill_uniform_kernel<<<std::min<long long>((count + 255) / 256, 4096), 256, 0, S->stream>>>(
+                p[0], count, r.seed, -0.1, 0.1);
+            step(cudaGetLastError(), "Generating c0");
+        }
+        step(cudaMemcpyAsync(p[1], p[0], f, cudaMemcpyDeviceToDevice, S->stream), "Copying c0");
+        if (e == cudaSuccess) ch_mass_kernel<<<1, 256, 0, S->stream>>>(p[0], (long long)r.n * r.n, S->mass_d);
+        step(cudaMemcpyAsync(&m, S->mass_d, sizeof(double), cudaMemcpyDeviceToHost, S->stream), "Reading mass");
+        step(cudaStreamSynchronize(S->stream), "Admitting");
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // clear a non-sticky error (an allocation failure is one)
+        for (double* q : p)
+            if (q) cudaFreeAsync(q, S->stream);
+        if (new_table) {
+            cudaFreeAsync(t.ptr, S->stream);
+            t.ptr = nullptr;
+        }
+        r.state = 3;
+        r.error = std::string("Error while '") + what + "': " + cudaGetErrorString(e);
+        r.done_t = now;
+        ++S->failed;
+        nvtxRangePop();
+        // a sticky error (the context is lost) ends the run; anything else stays with this request
+        const cudaError_t ctx = cudaStreamSynchronize(S->stream);
+        if (ctx != cudaSuccess) return srv_fail(ctx, "Admitting (device context lost)");
+        return kAdmitFailed;
+    }
+    if (new_table) S->used += (double)t.bytes;
+    ++t.refs;
     r.g.buf[S->parity] = p[0];        // cCurr
     r.g.buf[S->parity ^ 1] = p[1];    // cOld
     r.g.tmp = p[2];
     r.g.ends = p[3];
     r.g.tab = t.ptr;
     r.g.n = r.n;
-    if (!r.c0.empty()) {
-        SRV_TRY(cudaMemcpyAsync(p[0], r.c0.data(), f, cudaMemcpyHostToDevice, S->stream), "Uploading c0");
-    } else {
-        const long long count = (long long)r.n * r.n;
-        ch_fill_uniform_kernel<<<std::min<long long>((count + 255) / 256, 4096), 256, 0, S->stream>>>(
-            p[0], count, r.seed, -0.1, 0.1);
-        SRV_TRY(cudaGetLastError(), "Generating c0");
-    }
-    SRV_TRY(cudaMemcpyAsync(p[1], p[0], f, cudaMemcpyDeviceToDevice, S->stream), "Copying c0");
-    ch_mass_kernel<<<1, 256, 0, S->stream>>>(p[0], (long long)r.n * r.n, S->mass_d);
-    double m = 0.0;
-    SRV_TRY(cudaMemcpyAsync(&m, S->mass_d, sizeof(double), cudaMemcpyDeviceToHost, S->stream), "Reading mass");
-    SRV_TRY(cudaStreamSynchronize(S->stream), "Admitting");
     r.mean0 = m / ((double)r.n * r.n);
     r.bytes = grid_bytes(r.n);
     S->used += (double)r.bytes;
@@ -196,6 +244,7 @@ static int admit(Server* S, int id, double now) {
     r.remaining = r.steps;
     r.admit_t = now;
     S->active.push_back(id);
+    nvtxRangePop();
     return 0;
 }
 
@@ -248,6 +297,7 @@ static int run(Server* S) {
     size_t next = 0;   // first request (in arrival order) not yet admitted
     S->total_steps = 0;
     S->total_pt_steps = 0.0;
+    S->failed = 0;
     S->max_active = 0;
     S->max_used = S->used;
     int done = 0;
@@ -262,8 +312,12 @@ static int run(Server* S) {
             const double need = (double)grid_bytes(r.n);
             if (S->used + need > S->budget && !S->active.empty()) break;
             int st = admit(S, order[next], now());
-            if (st) return st;
             ++next;
+            if (st == kAdmitFailed) {
+                ++done;
+                continue;
+            }
+            if (st) return st;
             changed = true;
         }
         if (S->active.empty()) {
@@ -281,9 +335,11 @@ static int run(Server* S) {
         S->max_used = std::max(S->max_used, S->used);
         int k = S->chunk;
         for (int id : S->active) k = std::min(k, S->reqs[id].remaining);
+        nvtxRangePushA("chunk");
         int st = enqueue_steps(S, k);
         if (st) return st;
         SRV_TRY(cudaStreamSynchronize(S->stream), "Running a chunk");
+        nvtxRangePop();
         const double t_chunk = now();
         std::vector<int> still;
         bool retired = false;
@@ -293,7 +349,9 @@ static int run(Server* S) {
             S->total_steps += k;
             S->total_pt_steps += (double)k * r.n * r.n;
             if (r.remaining == 0) {
+                nvtxRangePushA("retire");
                 st = retire(S, id, t_chunk);
+                nvtxRangePop();
                 if (st) return st;
                 ++done;
                 retired = true;
@@ -350,6 +408,10 @@ int custen_ch_server_submit(void* h, int n, double lx, int steps, const double* 
                             double arrival, int* req_id) {
     Server* S = static_cast<Server*>(h);
     if (!S || n < 64 || n % BLK != 0 || steps < 1) return srv_arg("invalid request (n: multiple of 32, >= 64)");
+    const double need = (double)grid_bytes(n) + (double)tab_size(n) * sizeof(double);
+    if (need > S->budget)
+        return srv_arg("request of n = " + std::to_string(n) + " needs " + std::to_string((long long)need) +
+                       " bytes, above the server's HBM budget of " + std::to_string((long long)S->budget));
     Request r;
     r.n = n;
     r.lx = lx > 0 ? lx : 2.0 * M_PI;
@@ -376,6 +438,10 @@ int custen_ch_server_result(void* h, int id, double* c_out, double* arrival, dou
     Server* S = static_cast<Server*>(h);
     if (!S || id < 0 || id >= (int)S->reqs.size()) return srv_arg("invalid request id");
     const Request& r = S->reqs[id];
+    if (r.state == 3) {
+        g_srv_err = "request failed: " + r.error;
+        return 3;
+    }
     if (r.state != 2) return srv_arg("request not completed");
     if (c_out) {
         if (r.result.empty()) return srv_arg("results were not kept");
@@ -386,6 +452,23 @@ int custen_ch_server_result(void* h, int id, double* c_out, double* arrival, dou
     if (done_t) *done_t = r.done_t;
     if (mean0) *mean0 = r.mean0;
     if (mean_end) *mean_end = r.mean_end;
+    return 0;
+}
+
+// State of a request: 0 pending, 1 resident, 2 done, 3 failed (custen_ch_server_result reports why).
+int custen_ch_server_request_state(void* h, int id, int* state) {
+    Server* S = static_cast<Server*>(h);
+    if (!S || id < 0 || id >= (int)S->reqs.size() || !state) return srv_arg("invalid arguments");
+    *state = S->reqs[id].state;
+    return 0;
+}
+
+// Test hook for failure isolation: kind 1 makes the request's device allocation at admission fail with
+// cudaErrorMemoryAllocation (a fake of the failing call, on the host; nothing reaches the GPU).
+int custen_ch_server_inject_failure(void* h, int id, int kind) {
+    Server* S = static_cast<Server*>(h);
+    if (!S || id < 0 || id >= (int)S->reqs.size() || kind < 0 || kind > 1) return srv_arg("invalid arguments");
+    S->reqs[id].inject = kind;
     return 0;
 }
 

@@ -34,6 +34,7 @@
 
 #include "../../include/custen_gb300.h"
 #include "ch_internal.cuh"
+#include "checked.cuh"
 
 namespace custen {
 namespace ch {
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
 #pragma unroll 4
         for (int rr = warp; rr < BLK; rr += NW) {
             const T lap = fma(m_four, hh[rr + 1][j + 1], (hh[rr][j + 1] + hh[rr + 2][j + 1]) + (hh[rr + 1][j] + hh[rr + 1][j + 2]));
+            if (!in_bounds((long long)(y0 + rr) * n + x0 + j, 0, (long long)n * n)) continue;
             out[(size_t)rr * n] = (double)fma(m_two_thirds, dco[rr][j], lap);
         }
         __syncthreads();
@@ -192,7 +194,9 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
             }
             __syncwarp();
 #pragma unroll
-            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + il] = blk[rr][lane];
+            for (int rr = 0; rr < BLK; ++rr)
+                if (in_bounds((long long)(item.block * BLK + rr) * n + il, 0, (long long)n * n))
+                    rows[(size_t)rr * n + il] = blk[rr][lane];
             __syncwarp();
         }
         // backward substitution, chunks in reverse
@@ -225,7 +229,9 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
             }
             __syncwarp();
 #pragma unroll
-            for (int rr = 0; rr < BLK; ++rr) rows[(size_t)rr * n + il] = blk[rr][lane];
+            for (int rr = 0; rr < BLK; ++rr)
+                if (in_bounds((long long)(item.block * BLK + rr) * n + il, 0, (long long)n * n))
+                    rows[(size_t)rr * n + il] = blk[rr][lane];
             __syncwarp();
         }
         // the last two unknowns through the 2 x 2 Schur complement (BatchHyper.cu:195-227)
@@ -241,8 +247,10 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
         // kept apart as well: the y sweep overwrites columns n-2 and n-1 of tmp while other warps still
         // need them for the rank-2 correction
         const int gy = item.block * BLK + lane;
-        gd.ends[2 * gy] = x2;
-        gd.ends[2 * gy + 1] = x1;
+        if (in_bounds(2 * gy + 1, 0, 2 * n)) {
+            gd.ends[2 * gy] = x2;
+            gd.ends[2 * gy + 1] = x1;
+        }
     }
 }
 
@@ -317,7 +325,8 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
             }
 #pragma unroll
             for (int k = 0; k < CH; ++k)
-                if (yb + k < m) t[(size_t)(yb + k) * n + x] = v[k];
+                if (yb + k < m && in_bounds((long long)(yb + k) * n + x, 0, (long long)n * n))
+                    t[(size_t)(yb + k) * n + x] = v[k];
         }
         // backward substitution
         double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
@@ -345,7 +354,8 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
             }
 #pragma unroll
             for (int k = 0; k < CH; ++k)
-                if (yb + k < m) t[(size_t)(yb + k) * n + x] = v[k];
+                if (yb + k < m && in_bounds((long long)(yb + k) * n + x, 0, (long long)n * n))
+                    t[(size_t)(yb + k) * n + x] = v[k];
         }
         const double* om = tab + 7 * m;
         const double a = om[4], b = om[5], d = om[6], e = om[7];
@@ -354,6 +364,7 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
         const double x2 = om[0] * nx2 + om[1] * nx1;
         const double x1 = om[2] * nx2 + om[3] * nx1;
         // cNew = cBar + delta over cOld (cuPentCahnADI.cu:58-69, 89-100)
+        const double two = ((const volatile double*)g_rhs_factors)[0];   // register operand, as in K1
         const double* cur = parity ? gd.buf[1] : gd.buf[0];
         double* old = parity ? gd.buf[0] : gd.buf[1];
         for (int bb = 0; bb < nb; ++bb) {
@@ -374,15 +385,336 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
                 double dlt;
                 if (y < m) dlt = fma(-a1, x2, fma(-a2, x1, v[k]));
                 else dlt = (y == m) ? x2 : x1;
-                const double cbar = fma(2.0, cv[k], -ov[k]);
-                old[(size_t)y * n + x] = cbar + dlt;
+                const double cbar = fma(two, cv[k], -ov[k]);
+                if (in_bounds((long long)y * n + x, 0, (long long)n * n)) old[(size_t)y * n + x] = cbar + dlt;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// K2 / K3, pipelined: the same sweeps with the field values of chunk c+1 copied into shared memory
+// (cp.async, double buffered) while the recurrence runs over chunk c
+// ------------------------------------------------------------------------------------------------
+// The recurrences are latency-bound: a warp's chain issues one dependent FP64 operation at a time, so
+// the FP64 pipe stays busy only while other warps have work. In the kernels above a chunk's loads start
+// when its chain is about to run, and the values they stage in registers (32 per lane) limit the warps
+// per SM. Here the loads of the next chunk are in flight during the current chain, they occupy no
+// registers, and the table entries of the next chunk are read one chunk ahead. The arithmetic, its order
+// and so every result are those of the kernels above.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// x sweep (lane = row) over XC-column chunks. Each lane copies, and later writes back, the elements
+// e = lane + 32 j of a chunk (row e / XC, column e % XC): one row segment (XC = 32) or two (XC = 16) per
+// instruction, coalesced; a lane reads back in the backward pass exactly what it stored in the forward
+// pass, so program order alone orders those accesses.
+template <int XC>
+__global__ void __launch_bounds__(BLK) ch_xsolve_pipe_kernel(const GridDev* __restrict__ grids,
+                                                             const Item* __restrict__ items, int n_items,
+                                                             unsigned int* counter) {
+    __shared__ double blk[2][BLK][XC + 1];
+    __shared__ int s_item;
+    const int lane = threadIdx.x;
+    const unsigned FULL = 0xffffffffu;
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* tab = gd.tab;
+        const double* ds = tab;
+        const double* dl = tab + m;
+        const double* rd = tab + 2 * m;
+        const double* du = tab + 3 * m;
+        const double* dw = tab + 4 * m;
+        double* rows = gd.tmp + (size_t)item.block * BLK * n;   // 32 rows, stride n
+        const int nchunk = n / XC;
+        // element e = lane + 32 j sits at row j * RPI + lr, column lc of the chunk
+        constexpr int RPI = BLK / XC;
+        const int lr = lane / XC, lc = lane % XC;
+        const size_t step = (size_t)RPI * n;
+        auto issue = [&](int c, int b) {
+            const double* src = rows + (size_t)lr * n + c * XC + lc;
+#pragma unroll 4
+            for (int j = 0; j < XC; ++j, src += step) cp_async8(&blk[b][j * RPI + lr][lc], src);
+            cp_async_commit();
+        };
+        auto write_back = [&](int c, int b) {
+            double* dst = rows + (size_t)lr * n + c * XC + lc;
+#pragma unroll 4
+            for (int j = 0; j < XC; ++j, dst += step)
+                if (in_bounds(dst - gd.tmp, 0, (long long)n * n)) *dst = blk[b][j * RPI + lr][lc];
+        };
+        // forward elimination of the banded (n-2) x (n-2) block
+        double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
+        issue(0, 0);
+        double tds = lane < m ? ds[lane] : 0.0, tdl = lane < m ? dl[lane] : 0.0, trd = lane < m ? rd[lane] : 0.0;
+        for (int c = 0; c < nchunk; ++c) {
+            const int b = c & 1, cx = c * XC;
+            double nds = 0.0, ndl = 0.0, nrd = 0.0;
+            if (c + 1 < nchunk) {
+                issue(c + 1, b ^ 1);
+                const int il = cx + XC + lane;
+                if (il < m && lane < XC) { nds = ds[il]; ndl = dl[il]; nrd = rd[il]; }
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < XC; ++k) {
+                const int i = cx + k;
+                const double x = blk[b][lane][k];
+                const double a_s = __shfl_sync(FULL, tds, k), a_l = __shfl_sync(FULL, tdl, k);
+                const double a_r = __shfl_sync(FULL, trd, k);
+                if (i < m) {
+                    double t = fma(-a_s, b2, x);
+                    t = fma(-a_l, b1, t);
+                    t *= a_r;
+                    b2 = b1;
+                    b1 = t;
+                    blk[b][lane][k] = t;
+                } else if (i == m) {
+                    r2 = x;
+                } else {
+                    r1 = x;
+                }
+            }
+            __syncwarp();
+            write_back(c, b);
+            __syncwarp();   // buffer b is refilled next iteration
+            tds = nds; tdl = ndl; trd = nrd;
+        }
+        // backward substitution, chunks in reverse
+        double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
+        issue(nchunk - 1, 0);
+        int il0 = (nchunk - 1) * XC + lane;
+        double tdu = (il0 < m && lane < XC) ? du[il0] : 0.0, tdw = (il0 < m && lane < XC) ? dw[il0] : 0.0;
+        for (int j = 0; j < nchunk; ++j) {
+            const int c = nchunk - 1 - j, b = j & 1, cx = c * XC;
+            double ndu = 0.0, ndw = 0.0;
+            if (c > 0) {
+                issue(c - 1, b ^ 1);
+                const int il = cx - XC + lane;
+                if (il < m && lane < XC) { ndu = du[il]; ndw = dw[il]; }
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = XC - 1; k >= 0; --k) {
+                const int i = cx + k;
+                const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
+                if (i < m) {
+                    double y = fma(-a_u, f1, blk[b][lane][k]);
+                    y = fma(-a_w, f2, y);
+                    f2 = f1;
+                    f1 = y;
+                    blk[b][lane][k] = y;
+                    if (i == 0) y0v = y;
+                    if (i == 1) y1v = y;
+                    if (i == m - 2) ym2 = y;
+                    if (i == m - 1) ym1 = y;
+                }
+            }
+            __syncwarp();
+            write_back(c, b);
+            __syncwarp();
+            tdu = ndu; tdw = ndw;
+        }
+        // the last two unknowns through the 2 x 2 Schur complement (BatchHyper.cu:195-227)
+        const double* om = tab + 7 * m;
+        const double a = om[4], b = om[5], d = om[6], e = om[7];
+        const double nx2 = r2 - (e * y0v + a * ym2 + b * ym1);
+        const double nx1 = r1 - (d * y0v + e * y1v + a * ym1);
+        double* row = rows + (size_t)lane * n;
+        const double x2 = om[0] * nx2 + om[1] * nx1;
+        const double x1 = om[2] * nx2 + om[3] * nx1;
+        row[n - 2] = x2;
+        row[n - 1] = x1;
+        const int gy = item.block * BLK + lane;
+        if (in_bounds(2 * gy + 1, 0, 2 * n)) {
+            gd.ends[2 * gy] = x2;
+            gd.ends[2 * gy + 1] = x1;
+        }
+    }
+}
+
+// y sweep (lane = column) with CH-row batches copied one batch ahead. Each lane reads only its own
+// column, which it copied itself, so no warp barrier is needed around the buffers; results are stored
+// to global memory as the chain produces them. The update runs in register batches of 8 rows.
+template <int CH>
+__global__ void __launch_bounds__(BLK) ch_ysolve_pipe_kernel(const GridDev* __restrict__ grids,
+                                                             const Item* __restrict__ items, int n_items, int parity,
+                                                             unsigned int* counter) {
+    __shared__ double vb[2][CH][BLK];
+    __shared__ int s_item;
+    constexpr int UD = 8;
+    const int lane = threadIdx.x;
+    const unsigned FULL = 0xffffffffu;
+    const double two = ((const volatile double*)g_rhs_factors)[0];
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* tab = gd.tab;
+        const double* ds = tab;
+        const double* dl = tab + m;
+        const double* rd = tab + 2 * m;
+        const double* du = tab + 3 * m;
+        const double* dw = tab + 4 * m;
+        const double* inv1 = tab + 5 * m;
+        const double* inv2 = tab + 6 * m;
+        const int x = item.block * BLK + lane;
+        double* t = gd.tmp;
+        const double* ends = gd.ends;
+        const bool corr = x < m;
+        const double cx1 = corr ? inv1[x] : 0.0;
+        const double cx2 = corr ? inv2[x] : 0.0;
+        const int nb = n / CH;
+        auto issue = [&](int bb, int b, bool below_m) {
+            const int yb = bb * CH;
+            const double* src = t + (size_t)yb * n + x;
+#pragma unroll 4
+            for (int k = 0; k < CH; ++k, src += n)
+                if (!below_m || yb + k < m) cp_async8(&vb[b][k][lane], src);
+            cp_async_commit();
+        };
+        // forward elimination along y
+        double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
+        issue(0, 0, false);
+        double tds = 0.0, tdl = 0.0, trd = 0.0, e2 = 0.0, e1 = 0.0;
+        if (lane < CH) {
+            if (lane < m) { tds = ds[lane]; tdl = dl[lane]; trd = rd[lane]; }
+            e2 = ends[2 * lane];
+            e1 = ends[2 * lane + 1];
+        }
+        for (int bb = 0; bb < nb; ++bb) {
+            const int b = bb & 1, yb = bb * CH;
+            double nds = 0.0, ndl = 0.0, nrd = 0.0, ne2 = 0.0, ne1 = 0.0;
+            if (bb + 1 < nb) {
+                issue(bb + 1, b ^ 1, false);
+                const int yl = yb + CH + lane;
+                if (lane < CH) {
+                    if (yl < m) { nds = ds[yl]; ndl = dl[yl]; nrd = rd[yl]; }
+                    ne2 = ends[2 * yl];
+                    ne1 = ends[2 * yl + 1];
+                }
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+#pragma unroll
+            for (int k = 0; k < CH; ++k) {
+                const int y = yb + k;
+                const double c2 = __shfl_sync(FULL, e2, k), c1 = __shfl_sync(FULL, e1, k);
+                const double a_s = __shfl_sync(FULL, tds, k), a_l = __shfl_sync(FULL, tdl, k);
+                const double a_r = __shfl_sync(FULL, trd, k);
+                const double vk = vb[b][k][lane];
+                const double val = corr ? fma(-cx1, c2, fma(-cx2, c1, vk)) : vk;
+                if (y < m) {
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
+                    b2 = b1;
+                    b1 = w;
+                    if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
+                } else if (y == m) {
+                    r2 = val;
+                } else {
+                    r1 = val;
+                }
+            }
+            tds = nds; tdl = ndl; trd = nrd; e2 = ne2; e1 = ne1;
+        }
+        // backward substitution (rows below m only; the lane re-reads what it stored above)
+        double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
+        issue(nb - 1, 0, true);
+        int yl0 = (nb - 1) * CH + lane;
+        double tdu = (lane < CH && yl0 < m) ? du[yl0] : 0.0, tdw = (lane < CH && yl0 < m) ? dw[yl0] : 0.0;
+        for (int j = 0; j < nb; ++j) {
+            const int bb = nb - 1 - j, b = j & 1, yb = bb * CH;
+            double ndu = 0.0, ndw = 0.0;
+            if (bb > 0) {
+                issue(bb - 1, b ^ 1, true);
+                const int yl = yb - CH + lane;
+                if (lane < CH && yl < m) { ndu = du[yl]; ndw = dw[yl]; }
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+#pragma unroll
+            for (int k = CH - 1; k >= 0; --k) {
+                const int y = yb + k;
+                const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
+                if (y < m) {
+                    double w = fma(-a_u, f1, vb[b][k][lane]);
+                    w = fma(-a_w, f2, w);
+                    f2 = f1;
+                    f1 = w;
+                    if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
+                    if (y == m - 1) ym1 = w;
+                    if (y == m - 2) ym2 = w;
+                    if (y == 1) y1v = w;
+                    if (y == 0) y0v = w;
+                }
+            }
+            tdu = ndu; tdw = ndw;
+        }
+        const double* om = tab + 7 * m;
+        const double a = om[4], b = om[5], d = om[6], e = om[7];
+        const double nx2 = r2 - (e * y0v + a * ym2 + b * ym1);
+        const double nx1 = r1 - (d * y0v + e * y1v + a * ym1);
+        const double x2 = om[0] * nx2 + om[1] * nx1;
+        const double x1 = om[2] * nx2 + om[3] * nx1;
+        // cNew = cBar + delta over cOld (cuPentCahnADI.cu:58-69, 89-100)
+        const double* cur = parity ? gd.buf[1] : gd.buf[0];
+        double* old = parity ? gd.buf[0] : gd.buf[1];
+        for (int yb = 0; yb < n; yb += UD) {
+            const int yl = yb + (lane & (UD - 1));
+            const double ti1 = yl < m ? inv1[yl] : 0.0, ti2 = yl < m ? inv2[yl] : 0.0;
+            double v[UD], cv[UD], ov[UD];
+#pragma unroll
+            for (int k = 0; k < UD; ++k) {
+                const size_t q = (size_t)(yb + k) * n + x;
+                v[k] = (yb + k < m) ? t[q] : 0.0;
+                cv[k] = cur[q];
+                ov[k] = old[q];
+            }
+#pragma unroll
+            for (int k = 0; k < UD; ++k) {
+                const int y = yb + k;
+                const double a1 = __shfl_sync(FULL, ti1, k), a2 = __shfl_sync(FULL, ti2, k);
+                double dlt;
+                if (y < m) dlt = fma(-a1, x2, fma(-a2, x1, v[k]));
+                else dlt = (y == m) ? x2 : x1;
+                const double cbar = fma(two, cv[k], -ov[k]);
+                if (in_bounds((long long)y * n + x, 0, (long long)n * n)) old[(size_t)y * n + x] = cbar + dlt;
             }
         }
     }
 }
 
 ChConfig ch_config(int index) {
-    static const ChConfig tab[kChConfigs] = {{1, 32}, {2, 32}, {4, 32}, {1, 16}, {2, 16}, {4, 16}};
+    // {warps per right-hand-side CTA, y-sweep rows per batch, pipelined sweeps}
+    static const ChConfig tab[kChConfigs] = {{1, 32, 0}, {2, 32, 0}, {4, 32, 0}, {1, 16, 0}, {2, 16, 0},
+                                             {4, 16, 0}, {2, 16, 1}, {4, 16, 1}, {2, 32, 1}, {4, 32, 1}};
     return tab[(index >= 0 && index < kChConfigs) ? index : 0];
 }
 
@@ -406,6 +738,17 @@ cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grid
     else launch_rhs<double>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (c.pipe) {
+        // 64-100 registers and 8-17 KB of shared memory per one-warp CTA: up to 32 CTAs per SM
+        const int gp = std::max(1, std::min(n_rows, sms * 32));
+        if (c.y_chunk == 32) ch_xsolve_pipe_kernel<32><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+        else ch_xsolve_pipe_kernel<16><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (c.y_chunk == 32)
+            ch_ysolve_pipe_kernel<32><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+        else ch_ysolve_pipe_kernel<16><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+        return cudaGetLastError();
+    }
     ch_xsolve_kernel<<<g23, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (c.y_chunk == 32) ch_ysolve_kernel<32><<<g23, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
@@ -972,7 +1315,7 @@ int custen_ch_batch_autotune(void* h, int steps, char* name, size_t len) {
     b->cfg = best;
     if (name && len) {
         const ChConfig c = ch_config(best);
-        snprintf(name, len, "rhs_warps%d_ychunk%d", c.rhs_warps, c.y_chunk);
+        snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
     }
     return 0;
 }
@@ -994,7 +1337,7 @@ int custen_ch_batch_config(void* h, char* name, size_t len) {
     Batch* b = static_cast<Batch*>(h);
     if (!b || !name || !len) return ch_fail_arg("invalid arguments");
     const ChConfig c = batch_config(b);
-    snprintf(name, len, "rhs_warps%d_ychunk%d", c.rhs_warps, c.y_chunk);
+    snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
     return 0;
 }
 

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "builtin_funs.cuh"
+#include "checked.cuh"
 #include "custen_internal.h"
 
 namespace custen {
@@ -115,6 +116,7 @@ __device__ __forceinline__ void stage_tile_ldg(const StencilArgs& a, T* tile, co
         int c = (e - r * cvecs) * VEC;
         int gx = x0 - g.LP + c;
         const T* rowp = launch_row<T>(a, y0 - a.T + r);
+        if (!span_ok((long long)r * g.SW + c, VEC, (long long)g.SR * g.SW)) continue;
         T* dst = tile + r * g.SW + c;
         if (rowp == nullptr) {
 #pragma unroll
@@ -174,6 +176,7 @@ __device__ __forceinline__ void store_outputs(const StencilArgs& a, const T (&ac
         const int gyl = gy0 + rr;
         if (gyl >= a.rows) break;
         const int gy = a.row0 + gyl;
+        const bool row_ok = in_bounds(gyl, 0, a.rows);
         T* orow = reinterpret_cast<T*>(a.out) + (size_t)gyl * a.nx;
         int act[VEC];
         bool all_write = true;
@@ -194,12 +197,12 @@ __device__ __forceinline__ void store_outputs(const StencilArgs& a, const T (&ac
             T* o = reinterpret_cast<T*>(&outv);
 #pragma unroll
             for (int v = 0; v < VEC; ++v) o[v] = acc[rr][v];
-            *reinterpret_cast<V*>(orow + gx) = outv;
+            if (row_ok && span_ok(gx, VEC, a.nx)) *reinterpret_cast<V*>(orow + gx) = outv;
         } else {
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
-                if (act[v] == ACT_WRITE) orow[gx + v] = acc[rr][v];
-                else if (act[v] == ACT_ZERO) orow[gx + v] = T(0);
+                if (act[v] == ACT_SKIP || !row_ok || !in_bounds(gx + v, 0, a.nx)) continue;
+                orow[gx + v] = act[v] == ACT_WRITE ? acc[rr][v] : T(0);
             }
         }
     }
@@ -223,6 +226,8 @@ __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile,
     if (!is_fun) {
         for (int e = 0; e < nlist; ++e) {
             const T w = list_w[e];
+            if (!span_ok((long long)base + list_off[e], (long long)(RPT - 1) * g.SW + VEC, (long long)g.SR * g.SW))
+                continue;
             const T* p = tile + base + list_off[e];
 #pragma unroll
             for (int rr = 0; rr < RPT; ++rr)
@@ -236,6 +241,7 @@ __device__ __forceinline__ void compute_and_store(const StencilArgs& a, T* tile,
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
                 const int tl = base + rr * g.SW + v;    // window top-left
+                if (!span_ok(tl, (long long)(a.T + a.B) * g.SW + a.L + a.R + 1, (long long)g.SR * g.SW)) continue;
                 if (dir == 0) {
                     acc[rr][v] = reinterpret_cast<FunX<T>>(a.func)(tile, coef_s, tl + a.L);
                 } else if (dir == 1) {
@@ -300,6 +306,7 @@ __device__ __forceinline__ void compute_window_store(const StencilArgs& a, const
 #pragma unroll
     for (int k = 0; k < RPT + SH::V - 1; ++k) {
         T seg[NV * VEC];
+        if (!span_ok((long long)(r0 + k) * g.SW + c0, NV * VEC, (long long)g.SR * g.SW)) continue;
         const VV* src = reinterpret_cast<const VV*>(tile + (r0 + k) * g.SW + c0);
 #pragma unroll
         for (int q = 0; q < NV; ++q) {

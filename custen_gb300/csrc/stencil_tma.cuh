@@ -18,8 +18,7 @@
 
 namespace custen {
 
-extern __device__ unsigned int g_custen_device_error;
-constexpr unsigned int kErrMbarrierTimeout = 1u;
+constexpr unsigned int kErrMbarrierTimeout = 1u;   // g_custen_device_error: checked.cuh
 constexpr long long kWaitLimit = 1ll << 22;   // try_wait rounds (each may suspend ~µs) before giving up
 
 struct TmaMaps {
@@ -39,10 +38,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  : "memory");
 }
 
-// Bounded wait for the phase with the given parity to complete; false on expiry.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait for the phase with the given parity to complete; false after `limit` rounds.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kWaitLimit) {
     const uint32_t addr = smem_u32(bar);
-    for (long long i = 0; i < kWaitLimit; ++i) {
+    for (long long i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -114,6 +113,7 @@ __device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const 
             if (x >= 0 && x < a.nx) continue;
             const int xw = x < 0 ? x + a.nx : x - a.nx;
             if (xw < 0 || xw >= a.nx) continue;
+            if (!in_bounds((long long)r * g.SW + c, 0, (long long)g.SR * g.SW)) continue;
             tile[r * g.SW + c] = __ldg(reinterpret_cast<const T*>(a.in) + (size_t)gyl * a.nx + xw);
         }
     }

@@ -15,6 +15,7 @@
 // bit-identical to the reference's kernel on the same GPU.
 #include <cuda_runtime.h>
 
+#include "checked.cuh"
 #include "custen_internal.h"
 
 namespace custen {
@@ -133,6 +134,10 @@ __global__ void __launch_bounds__(kWenoThreads, 2) weno_adv_kernel(double* __res
         const double uu = uvel[q], vv = vvel[q];
         // Upwind side: the five differences are selected first and reconstructed once (two calls in a
         // conditional expression would let the compiler evaluate both and double the FP64 work).
+        if (!span_ok((long long)ty * kWenoDXW + tx, 6, (long long)kWenoTH * kWenoDXW) ||
+            !span_ok((long long)ty * kWenoTW + tx, 5 * kWenoTW + 1, (long long)kWenoDYH * kWenoTW) ||
+            !in_bounds((long long)q, 0, (long long)rows * nx))
+            continue;
         const double* dr = dxs + ty * kWenoDXW + tx;      // dr[k] = D at column x - 2 + k
         const bool ux = uu > 0.0;
         const double fx = weno5(k, ux ? dr[0] : dr[5], ux ? dr[1] : dr[4], dr[2 + !ux], ux ? dr[3] : dr[2],

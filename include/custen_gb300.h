@@ -157,9 +157,15 @@ int custen_builtin_function(int id, int dtype, void** func);
 int custen_probe_fma_rate(int dtype, double* fma_per_s);
 
 /* Device-side error flags raised by kernels instead of trapping (bit 0: a bounded mbarrier wait of a
- * TMA-staged kernel expired; the kernel then returned early). Synchronous; clear != 0 resets them.
- * No counterpart in the reference (its kernels have no waits). */
+ * TMA-staged kernel expired; the kernel then returned early. bit 1, in the checked build of the library
+ * only: a kernel index outside the extent it must stay in; that access was skipped). Synchronous;
+ * clear != 0 resets them. No counterpart in the reference (its kernels have no waits or checks). */
 int custen_device_error(unsigned int* flags, int clear);
+/* Self-test of that failure path: one CTA waits, with the stencil kernels' bounded wait limited to
+ * `rounds` try_wait rounds (1 .. 2^22), on an mbarrier nothing arrives on; the wait gives up, bit 0 is
+ * raised and the kernel returns. *flags receives the flags afterwards (left set). No copy fails and
+ * nothing traps; the context stays usable. */
+int custen_selftest_wait_expiry(long long rounds, unsigned int* flags);
 
 /* ---- batched pentadiagonal systems (cuPentBatch, cuPentCahnADI/src/cuPentBatch.cu) ----
  * Interleaved layout: element (row i, system s) of each diagonal and of b at [i * batch + s]; ds, dl
@@ -203,7 +209,7 @@ unsigned long long custen_ch_batch_launches(void* batch);
  * the fields, and keeps the fastest; results do not depend on it. No reference counterpart. */
 int custen_ch_batch_autotune(void* batch, int steps, char* name, size_t len);
 int custen_ch_batch_config(void* batch, char* name, size_t len);
-int custen_ch_batch_set_config(void* batch, int index);   /* 0 .. 5; -1: the default */
+int custen_ch_batch_set_config(void* batch, int index);   /* 0 .. 9; -1: the default */
 /* Checkpoint / resume of one grid through an HDF5 snapshot (the format below): save writes "c" = cCurr,
  * "c_old" = cOld and "t" = time; load takes "c" (must be n x n), "c_old" if present (else cCurr, as the
  * reference starts) and returns "t" in *time (NaN when absent, as in the reference's own snapshots).
@@ -241,6 +247,14 @@ int custen_ch_server_result(void* server, int request_id, double* c_out, double*
                             double* done_t, double* mean0, double* mean_end);
 int custen_ch_server_stats(void* server, double* makespan, long long* total_steps, double* total_point_steps,
                            int* max_active, double* peak_bytes, unsigned long long* launches);
+/* Failure isolation: a request whose admission fails (device allocation or upload) is marked failed
+ * (state 3; custen_ch_server_result returns 3 and the reason) and the run continues with the others; a
+ * request that can never fit the budget is rejected by submit. custen_ch_server_request_state: 0
+ * pending, 1 resident, 2 done, 3 failed. custen_ch_server_inject_failure is a test hook: kind 1 makes
+ * the request's admission allocation fail as cudaMallocAsync would on an exhausted device (a fake of
+ * the failing call on the host; nothing reaches the GPU). */
+int custen_ch_server_request_state(void* server, int request_id, int* state);
+int custen_ch_server_inject_failure(void* server, int request_id, int kind);
 int custen_ch_server_destroy(void* server);
 
 /* One Cahn-Hilliard step of one n x n grid that allocates nothing: for callers that cannot allocate

@@ -111,7 +111,7 @@ def test_fp32_stencil_variant_error_reported(gpu):
     b.close()
 
 
-CH_CONFIGS = 6
+CH_CONFIGS = 10
 
 
 def test_every_kernel_configuration_gives_identical_fields(gpu):
