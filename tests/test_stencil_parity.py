@@ -117,6 +117,17 @@ def test_parity_f32(gpu, variant):
 
 
 @pytest.mark.parametrize("variant", [cs.XP, cs.XNP, cs.YP, cs.YNP, cs.XYP, cs.XYNP])
+@pytest.mark.parametrize("tiles", [1, 3])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_parity_radius_4(gpu, variant, tiles, dtype):
+    """Radius-4 windows (X 9-point, Y 9-point, XY 9 x 9), numTiles 1 and 3."""
+    d = 0 if variant < 4 else (1 if variant < 8 else 2)
+    geom = {0: (9, 4, 4, 1, 0, 0), 1: (1, 0, 0, 9, 4, 4), 2: (9, 4, 4, 9, 4, 4)}[d]
+    got, ref, st, pre = run_both(variant, 96, 96, tiles, 32, 8, geom, dtype=dtype, seed=41 + variant + tiles)
+    check(got, ref, st, pre)
+
+
+@pytest.mark.parametrize("variant", [cs.XP, cs.XNP, cs.YP, cs.YNP, cs.XYP, cs.XYNP])
 def test_parity_unaligned_rows(gpu, variant):
     """nx = 98 doubles: rows are not 16-byte aligned, the scalar staging/store path runs."""
     d = 0 if variant < 4 else (1 if variant < 8 else 2)
