@@ -128,6 +128,10 @@ def lib() -> ctypes.CDLL:
         L.custen_ch_server_destroy.argtypes = [vp]
         L.custen_ch_server_request_state.argtypes = [vp, i, ctypes.POINTER(i)]
         L.custen_ch_server_inject_failure.argtypes = [vp, i, i]
+        L.custen_ch_server_set_snapshots.argtypes = [vp, i, i, ctypes.c_char_p]
+        L.custen_ch_server_submit_snapshot.argtypes = [vp, ctypes.c_char_p, ctypes.c_double, i, ctypes.c_double,
+                                                       ctypes.POINTER(i)]
+        L.custen_ch_server_snapshots_written.argtypes = [vp, i, ctypes.POINTER(i)]
         L.custen_ch_step_noalloc.argtypes = [vp, vp, vp, i, ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
         _lib = L
     return _lib
@@ -541,6 +545,25 @@ class CahnHilliardServer:
         st = ctypes.c_int()
         _srv_check(lib().custen_ch_server_request_state(self.h, rid, ctypes.byref(st)))
         return ("pending", "resident", "done", "failed")[st.value]
+
+    def snapshots(self, rid: int, every: int, directory) -> None:
+        """Write the request's state every `every` steps to directory/cahn_hilliard_<time>.nc."""
+        _srv_check(lib().custen_ch_server_set_snapshots(self.h, rid, int(every), os.fsencode(directory)))
+
+    def snapshots_written(self, rid: int) -> int:
+        c = ctypes.c_int()
+        _srv_check(lib().custen_ch_server_snapshots_written(self.h, rid, ctypes.byref(c)))
+        return c.value
+
+    def submit_snapshot(self, path, steps: int, arrival: float = 0.0, lx: float = 0.0) -> int:
+        """Queue a request resumed from a snapshot file; it advances `steps` more steps."""
+        rid = ctypes.c_int()
+        _srv_check(lib().custen_ch_server_submit_snapshot(self.h, os.fsencode(path), lx, steps, arrival,
+                                                          ctypes.byref(rid)))
+        dims = (ctypes.c_longlong * 2)()
+        lib().custen_h5_read(os.fsencode(path), b"c", None, 0, dims)
+        self.sizes.append(int(dims[0]))
+        return rid.value
 
     def inject_failure(self, rid: int, kind: int = 1) -> None:
         """Test hook: make the request's admission allocation fail (kind 1), on the host."""

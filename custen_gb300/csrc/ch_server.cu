@@ -54,6 +54,12 @@ struct Request {
     int state = 0;                   // 0 pending, 1 resident, 2 done, 3 failed (see error)
     int inject = 0;                  // test hook: 1 = the device allocation at admission fails
     std::string error;
+    std::vector<double> c_old0;      // host cOld to resume from (empty: cOld = c0, a fresh start)
+    double time = 0.0;               // simulated time, advanced by dt per step as the reference does
+    int done_steps = 0;
+    int snap_every = 0;              // write a snapshot every snap_every steps (0: none)
+    std::string snap_dir;
+    int snaps = 0;
     int remaining = 0;
     double admit_t = -1.0, done_t = -1.0;
     double mean0 = 0.0, mean_end = 0.0;
@@ -206,7 +212,10 @@ static int admit(Server* S, int id, double now) {
                 p[0], count, r.seed, -0.1, 0.1);
             step(cudaGetLastError(), "Generating c0");
         }
-        step(cudaMemcpyAsync(p[1], p[0], f, cudaMemcpyDeviceToDevice, S->stream), "Copying c0");
+        if (!r.c_old0.empty())
+            step(cudaMemcpyAsync(p[1], r.c_old0.data(), f, cudaMemcpyHostToDevice, S->stream), "Uploading cOld");
+        else
+            step(cudaMemcpyAsync(p[1], p[0], f, cudaMemcpyDeviceToDevice, S->stream), "Copying c0");
         if (e == cudaSuccess) ch_mass_kernel<<<1, 256, 0, S->stream>>>(p[0], (long long)r.n * r.n, S->mass_d);
         step(cudaMemcpyAsync(&m, S->mass_d, sizeof(double), cudaMemcpyDeviceToHost, S->stream), "Reading mass");
         step(cudaStreamSynchronize(S->stream), "Admitting");
@@ -274,6 +283,55 @@ static int retire(Server* S, int id, double now_after) {
     return 0;
 }
 
+// Snapshot of a resident request after its done_steps-th step: the reference's Print_Out file
+// (cuPentCahnADI.cu:103-140, name cahn_hilliard_<time %0.10lf>.nc, dataset "c") with "c_old" and "t"
+// added so that the request can be resumed (custen_ch_server_submit_snapshot). Returns false with
+// *err set when reading back or writing fails.
+static bool write_snapshot(Server* S, Request& r, std::string* err) {
+    const size_t count = (size_t)r.n * r.n;
+    std::vector<double> cur(count), old(count);
+    cudaError_t e = cudaMemcpyAsync(cur.data(), r.g.buf[S->parity], count * sizeof(double), cudaMemcpyDeviceToHost,
+                                    S->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(old.data(), r.g.buf[S->parity ^ 1], count * sizeof(double), cudaMemcpyDeviceToHost,
+                            S->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+    if (e != cudaSuccess) {
+        *err = std::string("Error while 'Reading a snapshot': ") + cudaGetErrorString(e);
+        return false;
+    }
+    char num[64];
+    snprintf(num, sizeof(num), "%0.10f", r.time);
+    const std::string path = r.snap_dir + "/cahn_hilliard_" + num + ".nc";
+    const char* names[3] = {"c", "c_old", "t"};
+    const double* data[3] = {cur.data(), old.data(), &r.time};
+    const long long dims[6] = {r.n, r.n, r.n, r.n, 1, 1};
+    if (custen_h5_write(path.c_str(), 3, names, data, dims) != 0) {
+        *err = std::string("Error while 'Writing a snapshot': ") + custen_h5_last_error();
+        return false;
+    }
+    ++r.snaps;
+    return true;
+}
+
+// Take a resident request out of the run as failed: release its memory, record why.
+static int drop(Server* S, int id, const std::string& why, double now) {
+    Request& r = S->reqs[id];
+    for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends}) SRV_TRY(cudaFreeAsync(p, S->stream), "Freeing a grid");
+    S->used -= (double)r.bytes;
+    TableRef& t = S->tables[r.table_key];
+    if (--t.refs == 0) {
+        SRV_TRY(cudaFreeAsync(t.ptr, S->stream), "Freeing a table");
+        S->used -= (double)t.bytes;
+        t.ptr = nullptr;
+    }
+    r.state = 3;
+    r.error = why;
+    r.done_t = now;
+    ++S->failed;
+    return 0;
+}
+
 static int enqueue_steps(Server* S, int k) {
     for (int s = 0; s < k; ++s) {
         SRV_TRY(cudaMemsetAsync(S->counters, 0, 3 * sizeof(unsigned int), S->stream), "Resetting counters");
@@ -334,7 +392,11 @@ static int run(Server* S) {
         S->max_active = std::max<int>(S->max_active, (int)S->active.size());
         S->max_used = std::max(S->max_used, S->used);
         int k = S->chunk;
-        for (int id : S->active) k = std::min(k, S->reqs[id].remaining);
+        for (int id : S->active) {
+            const Request& r = S->reqs[id];
+            k = std::min(k, r.remaining);
+            if (r.snap_every > 0) k = std::min(k, r.snap_every - r.done_steps % r.snap_every);
+        }
         nvtxRangePushA("chunk");
         int st = enqueue_steps(S, k);
         if (st) return st;
@@ -346,8 +408,23 @@ static int run(Server* S) {
         for (int id : S->active) {
             Request& r = S->reqs[id];
             r.remaining -= k;
+            r.done_steps += k;
+            const double dt = S->dt_factor * (r.lx / r.n);   // dx = lx / n, dt = dt_factor * dx
+            for (int q = 0; q < k; ++q) r.time += dt;
             S->total_steps += k;
             S->total_pt_steps += (double)k * r.n * r.n;
+            if (r.snap_every > 0 && r.done_steps % r.snap_every == 0) {
+                nvtxRangePushA("snapshot");
+                std::string err;
+                const bool ok = write_snapshot(S, r, &err);
+                nvtxRangePop();
+                if (!ok) {
+                    if ((st = drop(S, id, err, t_chunk))) return st;
+                    ++done;
+                    retired = true;
+                    continue;
+                }
+            }
             if (r.remaining == 0) {
                 nvtxRangePushA("retire");
                 st = retire(S, id, t_chunk);
@@ -452,6 +529,59 @@ int custen_ch_server_result(void* h, int id, double* c_out, double* arrival, dou
     if (done_t) *done_t = r.done_t;
     if (mean0) *mean0 = r.mean0;
     if (mean_end) *mean_end = r.mean_end;
+    return 0;
+}
+
+// Periodic snapshots of a request (before run): every `every` steps (0: none) its state is written to
+// dir/cahn_hilliard_<time %0.10f>.nc, the reference's Print_Out file (cuPentCahnADI.cu:103-140,
+// 585-595) with "c_old" and "t" added; chunks end on those steps. A failed write fails the request.
+int custen_ch_server_set_snapshots(void* h, int id, int every, const char* dir) {
+    Server* S = static_cast<Server*>(h);
+    if (!S || id < 0 || id >= (int)S->reqs.size() || every < 0 || (every > 0 && (!dir || !dir[0])))
+        return srv_arg("invalid arguments");
+    if (S->reqs[id].state != 0) return srv_arg("request already started");
+    S->reqs[id].snap_every = every;
+    S->reqs[id].snap_dir = every > 0 ? dir : "";
+    return 0;
+}
+
+// Queue a request resumed from a snapshot: the grid and cCurr from "c" (n x n), cOld from "c_old" when
+// present (else cCurr, a fresh start as in the reference), the simulated time from "t" (else 0); it
+// advances `steps` more steps. A snapshot this server wrote resumes bit for bit.
+int custen_ch_server_submit_snapshot(void* h, const char* path, double lx, int steps, double arrival, int* req_id) {
+    Server* S = static_cast<Server*>(h);
+    if (!S || !path) return srv_arg("invalid arguments");
+    long long dims[2] = {0, 0};
+    if (custen_h5_read(path, "c", nullptr, 0, dims) != 0) return srv_arg(std::string("Reading the snapshot: ") + custen_h5_last_error());
+    if (dims[0] != dims[1] || dims[0] > (1 << 20)) return srv_arg("snapshot field is not a square grid");
+    const int n = (int)dims[0];
+    std::vector<double> c((size_t)n * n), old;
+    if (custen_h5_read(path, "c", c.data(), (long long)c.size(), dims) != 0)
+        return srv_arg(std::string("Reading the snapshot: ") + custen_h5_last_error());
+    long long od[2];
+    if (custen_h5_read(path, "c_old", nullptr, 0, od) == 0) {
+        if (od[0] != n || od[1] != n) return srv_arg("snapshot c_old does not match c");
+        old.resize(c.size());
+        if (custen_h5_read(path, "c_old", old.data(), (long long)old.size(), od) != 0)
+            return srv_arg(std::string("Reading the snapshot: ") + custen_h5_last_error());
+    }
+    double t = 0.0;
+    long long td[2];
+    if (custen_h5_read(path, "t", nullptr, 0, td) == 0 && td[0] * td[1] == 1) custen_h5_read(path, "t", &t, 1, td);
+    int id = -1;
+    const int st = custen_ch_server_submit(h, n, lx, steps, c.data(), 0, arrival, &id);
+    if (st) return st;
+    S->reqs[id].c_old0 = std::move(old);
+    S->reqs[id].time = t;
+    if (req_id) *req_id = id;
+    return 0;
+}
+
+// Snapshots a request has written so far.
+int custen_ch_server_snapshots_written(void* h, int id, int* count) {
+    Server* S = static_cast<Server*>(h);
+    if (!S || id < 0 || id >= (int)S->reqs.size() || !count) return srv_arg("invalid arguments");
+    *count = S->reqs[id].snaps;
     return 0;
 }
 

@@ -254,6 +254,16 @@ int custen_ch_server_stats(void* server, double* makespan, long long* total_step
  * the request's admission allocation fail as cudaMallocAsync would on an exhausted device (a fake of
  * the failing call on the host; nothing reaches the GPU). */
 int custen_ch_server_request_state(void* server, int request_id, int* state);
+/* Checkpoint / resume in the server. custen_ch_server_set_snapshots (before run): every `every` steps
+ * the request's state goes to dir/cahn_hilliard_<time %0.10f>.nc -- the reference's Print_Out file
+ * (cuPentCahnADI.cu:103-140, 585-595: dataset "c", time accumulated by dt per step) plus "c_old" and
+ * "t"; a failed write fails the request. custen_ch_server_submit_snapshot queues a request resumed
+ * from such a file (n and cCurr from "c", cOld from "c_old" or cCurr, time from "t" or 0), which then
+ * continues bit for bit; lx <= 0 means 2 pi. */
+int custen_ch_server_set_snapshots(void* server, int request_id, int every, const char* dir);
+int custen_ch_server_submit_snapshot(void* server, const char* path, double lx, int steps, double arrival,
+                                     int* request_id);
+int custen_ch_server_snapshots_written(void* server, int request_id, int* count);
 int custen_ch_server_inject_failure(void* server, int request_id, int kind);
 int custen_ch_server_destroy(void* server);
 
