@@ -858,7 +858,11 @@ def run_ch_batched(args, cs):
             b.set_state(k, crng.uniform(-0.1, 0.1, (n, n)))
         b.step(2)
         b.synchronize()
-        cfg_name = b.autotune(steps=4) if args.autotune else b.config()   # state restored by the tuner
+        if args.ch_config >= 0:
+            b.set_config(args.ch_config)
+            cfg_name = b.config()
+        else:
+            cfg_name = b.autotune(steps=4) if args.autotune else b.config()   # state restored by the tuner
         l0 = b.launches()
         t0 = time.perf_counter()
         b.step(steps)
@@ -960,6 +964,8 @@ def main():
     ap.add_argument("--skip-indirect", action="store_true")
     ap.add_argument("--skip-pent", action="store_true")
     ap.add_argument("--pent-batch", type=int, default=1 << 18, help="systems in the pentadiagonal leg (256 unknowns each)")
+    ap.add_argument("--ch-config", type=int, default=-1,
+                    help="pin the CH batch kernel configuration (0..9) instead of tuning it")
     ap.add_argument("--stage-chunk-mb", type=int, default=0,
                     help="chunk size of the host-memory staging path (0: the library default)")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],

@@ -21,6 +21,7 @@
 #include <mutex>
 #include <string>
 #include <sys/stat.h>
+#include <unistd.h>
 #include <vector>
 
 #include "stencil_configs.h"
@@ -101,7 +102,8 @@ void mkdirs(const std::string& path) {
 void save() {
     const std::string& path = cache_path();
     mkdirs(path);
-    const std::string tmp = path + ".tmp";
+    // a per-process temporary, renamed over the cache: concurrent writers never interleave
+    const std::string tmp = path + "." + std::to_string((long long)getpid()) + ".tmp";
     FILE* f = fopen(tmp.c_str(), "w");
     if (!f) return;
     fprintf(f, "{\n\"custen_gb300_tune_cache\": 1,\n\"entries\": {\n");
@@ -113,15 +115,16 @@ void save() {
         fprintf(f, "]}%s\n", ++k < g_cache.size() ? "," : "");
     }
     fprintf(f, "}\n}\n");
-    fclose(f);
-    rename(tmp.c_str(), path.c_str());
+    if (fclose(f) != 0 || rename(tmp.c_str(), path.c_str()) != 0) remove(tmp.c_str());
 }
 
 std::string gpu_name() {
     static std::string names[64];
+    static std::mutex mu;
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return "gpu";
+    std::lock_guard<std::mutex> lock(mu);
     if (names[dev].empty()) {
         cudaDeviceProp prop;
         names[dev] = cudaGetDeviceProperties(&prop, dev) == cudaSuccess ? prop.name : "gpu";

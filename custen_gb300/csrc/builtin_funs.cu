@@ -1,6 +1,9 @@
 // Device-function pointers of the shipped Fun functions (builtin_funs.cuh) and their C-ABI lookup.
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "builtin_funs.cuh"
 
 #include "../../include/custen_gb300.h"
@@ -72,15 +75,21 @@ extern "C" int custen_builtin_function(int id, int dtype, void** func) {
 // Which shipped function `f` is on the current device (0..5), or -1. The twelve addresses are read once
 // per device.
 extern "C" int custen_builtin_fun_id(const void* f, int dtype) {
+    // filled once per device under the mutex; the flag publishes the filled table to other threads
     static void* cache[64][2][6];
-    static bool ready[64] = {};
+    static std::atomic<bool> ready[64] = {};
+    static std::mutex mu;
     int dev = 0;
     if (f == nullptr || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
-    if (!ready[dev]) {
-        for (int t = 0; t < 2; ++t)
-            for (int id = 0; id < 6; ++id)
-                if (custen_builtin_function(id, t == 0 ? CUSTEN_F64 : CUSTEN_F32, &cache[dev][t][id]) != 0) return -1;
-        ready[dev] = true;
+    if (!ready[dev].load(std::memory_order_acquire)) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!ready[dev].load(std::memory_order_relaxed)) {
+            for (int t = 0; t < 2; ++t)
+                for (int id = 0; id < 6; ++id)
+                    if (custen_builtin_function(id, t == 0 ? CUSTEN_F64 : CUSTEN_F32, &cache[dev][t][id]) != 0)
+                        return -1;
+            ready[dev].store(true, std::memory_order_release);
+        }
     }
     const int t = dtype == CUSTEN_F64 ? 0 : 1;
     for (int id = 0; id < 6; ++id)

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -964,7 +965,7 @@ static __device__ __align__(256) unsigned char g_ch_noalloc_scratch[kNoAllocByte
 
 // Device address of the array for each device, taken once with that device current. In host code the
 // array's name is only a host-side stand-in, never a device address.
-static unsigned char* g_noalloc_base[64] = {};
+static std::atomic<unsigned char*> g_noalloc_base[64] = {};
 
 }  // namespace ch
 }  // namespace custen
@@ -1194,12 +1195,13 @@ int custen_ch_step_noalloc(const double* c_old, const double* c_cur, double* c_n
     int dev = 0;
     CH_TRY(cudaGetDevice(&dev), "Querying the current device");
     if (dev < 0 || dev >= 64) return ch_fail_arg("custen_ch_step_noalloc: device index out of range");
-    if (g_noalloc_base[dev] == nullptr) {
+    unsigned char* base = g_noalloc_base[dev].load(std::memory_order_acquire);
+    if (base == nullptr) {   // the same address whichever thread looks it up first
         void* p = nullptr;
         CH_TRY(cudaGetSymbolAddress(&p, g_ch_noalloc_scratch), "Looking up the scratch array's device address");
-        g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+        base = static_cast<unsigned char*>(p);
+        g_noalloc_base[dev].store(base, std::memory_order_release);
     }
-    unsigned char* base = g_noalloc_base[dev];
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // host-side inputs in stack buffers (no heap either)

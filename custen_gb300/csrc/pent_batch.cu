@@ -17,6 +17,8 @@
 // variant is bound by HBM.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <algorithm>
 #include <cstdio>
 #include <string>
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) invert_kernel(double* __restrict__ d
 }
 
 thread_local std::string g_err;
-int g_kr[3] = {8, 2, 2};   // prefetch depth: factor, exact solve, inverted-pivot solve (measured best)
+std::atomic<int> g_kr[3] = {8, 2, 2};   // prefetch depth: factor, exact solve, inverted-pivot solve (measured best)
 
 template <typename F2, typename F4, typename F8>
 void by_depth(int kr, F2 f2, F4 f4, F8 f8) {

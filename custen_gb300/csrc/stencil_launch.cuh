@@ -4,6 +4,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "stencil_kernel.cuh"
@@ -39,13 +40,16 @@ stencil_ldg_kernel(const __grid_constant__ StencilArgs a) {
 
 // Largest dynamic shared memory a block may opt in to on the current device.
 inline int smem_optin_limit() {
-    static int cached[64] = {};
+    static std::atomic<int> cached[64] = {};   // threads that race store the same value
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+    if (dev >= 0 && dev < 64) {
+        const int c = cached[dev].load(std::memory_order_relaxed);
+        if (c) return c;
+    }
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) v = 48 * 1024;
-    if (dev >= 0 && dev < 64) cached[dev] = v;
+    if (dev >= 0 && dev < 64) cached[dev].store(v, std::memory_order_relaxed);
     return v;
 }
 
@@ -102,13 +106,16 @@ inline bool encode_rows_map(CUtensorMap* m, const void* base, int nx, int rows, 
 }
 
 inline int sm_count() {
-    static int cached[64] = {};
+    static std::atomic<int> cached[64] = {};   // threads that race store the same value
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+    if (dev >= 0 && dev < 64) {
+        const int c = cached[dev].load(std::memory_order_relaxed);
+        if (c) return c;
+    }
     int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    if (dev >= 0 && dev < 64) cached[dev] = v;
+    if (dev >= 0 && dev < 64) cached[dev].store(v, std::memory_order_relaxed);
     return v;
 }
 

@@ -15,6 +15,8 @@
 // bit-identical to the reference's kernel on the same GPU.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "checked.cuh"
 #include "custen_internal.h"
 
@@ -155,14 +157,15 @@ __global__ void __launch_bounds__(kWenoThreads, 2) weno_adv_kernel(double* __res
 }  // namespace
 
 cudaError_t launch_weno_adv(const StencilArgs& a, cudaStream_t s) {
-    static bool attr_set[64] = {};
+    // setting the attribute is idempotent: threads that race here both set it
+    static std::atomic<bool> attr_set[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
         e = cudaFuncSetAttribute(weno_adv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWenoSmem);
         if (e != cudaSuccess) return e;
-        attr_set[dev] = true;
+        attr_set[dev].store(true, std::memory_order_release);
     }
     if (a.rows <= 0 || a.nx <= 0) return cudaSuccess;
     dim3 grid((a.nx + kWenoTW - 1) / kWenoTW, (a.rows + kWenoTH - 1) / kWenoTH);

@@ -351,3 +351,33 @@ def test_parity_shape_kernels(gpu, shape, dtype, dense):
     s.destroy()
     assert cs.kernel_launches_tma() > before
     check(got, ref, st, pre)
+
+
+def test_concurrent_handles_from_host_threads(gpu):
+    """Independent handles driven from four host threads at once (ctypes releases the GIL during each
+    call): the lazily filled per-device tables (device-function addresses, kernel attributes, device
+    properties) are shared safely and every result matches the oracle."""
+    import threading
+
+    cases = [(cs.XYPFUN, (3, 1, 1, 3, 1, 1), FUN_IDS[2][1]), (cs.XNP, (5, 2, 2, 1, 0, 0), -1),
+             (cs.YPFUN, (1, 0, 0, 5, 2, 2), FUN_IDS[1][1]), (cs.XYNP, (5, 2, 2, 5, 2, 2), -1)]
+    errors = []
+
+    def worker(k):
+        try:
+            cs._check(cs.lib().custen_set_device(0))
+            variant, geom, fun_id = cases[k]
+            d = 0 if variant < 4 else (1 if variant < 8 else 2)
+            for rep in range(3):
+                got, ref, st, pre = run_both(variant, 128, 64, 2, 32 if d != 1 else 16, 8, geom, fun_id=fun_id,
+                                             seed=100 + 10 * k + rep)
+                check(got, ref, st, pre)
+        except Exception as e:  # reported on the main thread
+            errors.append(f"thread {k}: {e!r}")
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not errors, errors
