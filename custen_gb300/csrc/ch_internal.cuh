@@ -40,16 +40,20 @@ __global__ void ch_mass_kernel(const double* __restrict__ f, long long count, do
 
 // Kernel configuration of a step: warps per right-hand-side CTA (1, 2, 4), rows per batch of the y
 // sweep (16, 32; with pipelined sweeps also the x sweep's columns per chunk), and whether the sweeps
-// copy the next chunk into shared memory while the current one runs. Every configuration computes the
-// same values; the batch tuner times them.
+// copy the next chunk into shared memory while the current one runs (pipe 1; pipe 2: the x sweep takes
+// x_chunk-column chunks with its table entries in registers; pipe 3: both sweeps hold their table
+// entries in registers, the y sweep in y_chunk-row batches). Every configuration computes the same values; the
+// batch tuner times them.
 struct ChConfig {
     int rhs_warps;
     int y_chunk;
     int pipe;
+    int x_chunk;   // columns per chunk of the register-table x sweep (pipe 2, 3): 8 or 16
 };
-constexpr ChConfig kChDefault{4, 16, 0};
-constexpr int kChConfigs = 10;
+constexpr ChConfig kChDefault{4, 8, 3, 16};   // configuration 12, the fastest at 512 mixed grids
+constexpr int kChConfigs = 17;
 ChConfig ch_config(int index);   // 0 .. kChConfigs-1
+void config_name(const ChConfig& c, char* name, size_t len);
 
 // One step of every grid of a work list: right-hand side, x sweep, y sweep (3 launches on s).
 // counters: 3 zeroed work counters.

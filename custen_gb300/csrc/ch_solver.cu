@@ -552,6 +552,142 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_pipe_kernel(const GridDev* __re
     }
 }
 
+// The same x sweep with XC-column chunks (8 or 16) whose table entries every lane holds in registers, read with
+// uniform (broadcast) loads when the chunk starts and before its field copies are awaited: the chain
+// then takes no shuffle. The arithmetic is that of the kernels above.
+template <int XC>
+__global__ void __launch_bounds__(BLK) ch_xsolve_pipe_rt_kernel(const GridDev* __restrict__ grids,
+                                                                const Item* __restrict__ items, int n_items,
+                                                                unsigned int* counter) {
+    constexpr int RPI = BLK / XC;
+    __shared__ double blk[2][BLK][XC + 1];
+    __shared__ int s_item;
+    const int lane = threadIdx.x;
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* tab = gd.tab;
+        const double* ds = tab;
+        const double* dl = tab + m;
+        const double* rd = tab + 2 * m;
+        const double* du = tab + 3 * m;
+        const double* dw = tab + 4 * m;
+        double* rows = gd.tmp + (size_t)item.block * BLK * n;
+        const int nchunk = n / XC;
+        const int lr = lane / XC, lc = lane % XC;
+        const size_t step = (size_t)RPI * n;
+        auto issue = [&](int c, int b) {
+            const double* src = rows + (size_t)lr * n + c * XC + lc;
+#pragma unroll 4
+            for (int j = 0; j < XC; ++j, src += step) cp_async8(&blk[b][j * RPI + lr][lc], src);
+            cp_async_commit();
+        };
+        auto write_back = [&](int c, int b) {
+            double* dst = rows + (size_t)lr * n + c * XC + lc;
+#pragma unroll 4
+            for (int j = 0; j < XC; ++j, dst += step)
+                if (in_bounds(dst - gd.tmp, 0, (long long)n * n)) *dst = blk[b][j * RPI + lr][lc];
+        };
+        double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
+        issue(0, 0);
+        for (int c = 0; c < nchunk; ++c) {
+            const int b = c & 1, cx = c * XC;
+            double ts[XC], tl[XC], tr[XC];
+#pragma unroll
+            for (int k = 0; k < XC; ++k) {
+                const bool in = cx + k < m;
+                ts[k] = in ? __ldg(ds + cx + k) : 0.0;
+                tl[k] = in ? __ldg(dl + cx + k) : 0.0;
+                tr[k] = in ? __ldg(rd + cx + k) : 0.0;
+            }
+            if (c + 1 < nchunk) {
+                issue(c + 1, b ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < XC; ++k) {
+                const int i = cx + k;
+                const double x = blk[b][lane][k];
+                if (i < m) {
+                    double t = fma(-ts[k], b2, x);
+                    t = fma(-tl[k], b1, t);
+                    t *= tr[k];
+                    b2 = b1;
+                    b1 = t;
+                    blk[b][lane][k] = t;
+                } else if (i == m) {
+                    r2 = x;
+                } else {
+                    r1 = x;
+                }
+            }
+            __syncwarp();
+            write_back(c, b);
+            __syncwarp();
+        }
+        double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
+        issue(nchunk - 1, 0);
+        for (int j = 0; j < nchunk; ++j) {
+            const int c = nchunk - 1 - j, b = j & 1, cx = c * XC;
+            double tu[XC], tw[XC];
+#pragma unroll
+            for (int k = 0; k < XC; ++k) {
+                const bool in = cx + k < m;
+                tu[k] = in ? __ldg(du + cx + k) : 0.0;
+                tw[k] = in ? __ldg(dw + cx + k) : 0.0;
+            }
+            if (c > 0) {
+                issue(c - 1, b ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = XC - 1; k >= 0; --k) {
+                const int i = cx + k;
+                if (i < m) {
+                    double y = fma(-tu[k], f1, blk[b][lane][k]);
+                    y = fma(-tw[k], f2, y);
+                    f2 = f1;
+                    f1 = y;
+                    blk[b][lane][k] = y;
+                    if (i == 0) y0v = y;
+                    if (i == 1) y1v = y;
+                    if (i == m - 2) ym2 = y;
+                    if (i == m - 1) ym1 = y;
+                }
+            }
+            __syncwarp();
+            write_back(c, b);
+            __syncwarp();
+        }
+        const double* om = tab + 7 * m;
+        const double a = om[4], bq = om[5], d = om[6], e = om[7];
+        const double nx2 = r2 - (e * y0v + a * ym2 + bq * ym1);
+        const double nx1 = r1 - (d * y0v + e * y1v + a * ym1);
+        double* row = rows + (size_t)lane * n;
+        const double x2 = om[0] * nx2 + om[1] * nx1;
+        const double x1 = om[2] * nx2 + om[3] * nx1;
+        row[n - 2] = x2;
+        row[n - 1] = x1;
+        const int gy = item.block * BLK + lane;
+        if (in_bounds(2 * gy + 1, 0, 2 * n)) {
+            gd.ends[2 * gy] = x2;
+            gd.ends[2 * gy + 1] = x1;
+        }
+    }
+}
+
 // y sweep (lane = column) with CH-row batches copied one batch ahead. Each lane reads only its own
 // column, which it copied itself, so no warp barrier is needed around the buffers; results are stored
 // to global memory as the chain produces them. The update runs in register batches of 8 rows.
@@ -712,11 +848,182 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_pipe_kernel(const GridDev* __re
     }
 }
 
+// The same y sweep with the batch's table entries (pivots, multipliers, x-sweep row ends, update
+// factors) held in registers by every lane, read with uniform loads before the batch's copies are
+// awaited: the chain takes no shuffle. The arithmetic is that of the kernels above.
+template <int CH>
+__global__ void __launch_bounds__(BLK) ch_ysolve_pipe_rt_kernel(const GridDev* __restrict__ grids,
+                                                             const Item* __restrict__ items, int n_items, int parity,
+                                                             unsigned int* counter) {
+    __shared__ double vb[2][CH][BLK];
+    __shared__ int s_item;
+    constexpr int UD = 8;
+    const int lane = threadIdx.x;
+    const double two = ((const volatile double*)g_rhs_factors)[0];
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* tab = gd.tab;
+        const double* ds = tab;
+        const double* dl = tab + m;
+        const double* rd = tab + 2 * m;
+        const double* du = tab + 3 * m;
+        const double* dw = tab + 4 * m;
+        const double* inv1 = tab + 5 * m;
+        const double* inv2 = tab + 6 * m;
+        const int x = item.block * BLK + lane;
+        double* t = gd.tmp;
+        const double* ends = gd.ends;
+        const bool corr = x < m;
+        const double cx1 = corr ? inv1[x] : 0.0;
+        const double cx2 = corr ? inv2[x] : 0.0;
+        const int nb = n / CH;
+        auto issue = [&](int bb, int b, bool below_m) {
+            const int yb = bb * CH;
+            const double* src = t + (size_t)yb * n + x;
+#pragma unroll 4
+            for (int k = 0; k < CH; ++k, src += n)
+                if (!below_m || yb + k < m) cp_async8(&vb[b][k][lane], src);
+            cp_async_commit();
+        };
+        // forward elimination along y
+        double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
+        issue(0, 0, false);
+        for (int bb = 0; bb < nb; ++bb) {
+            const int b = bb & 1, yb = bb * CH;
+            double ts[CH], tl[CH], tr[CH], te2[CH], te1[CH];
+#pragma unroll
+            for (int k = 0; k < CH; ++k) {
+                const bool in = yb + k < m;
+                ts[k] = in ? __ldg(ds + yb + k) : 0.0;
+                tl[k] = in ? __ldg(dl + yb + k) : 0.0;
+                tr[k] = in ? __ldg(rd + yb + k) : 0.0;
+                te2[k] = ends[2 * (yb + k)];
+                te1[k] = ends[2 * (yb + k) + 1];
+            }
+            if (bb + 1 < nb) {
+                issue(bb + 1, b ^ 1, false);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+#pragma unroll
+            for (int k = 0; k < CH; ++k) {
+                const int y = yb + k;
+                const double c2 = te2[k], c1 = te1[k];
+                const double a_s = ts[k], a_l = tl[k];
+                const double a_r = tr[k];
+                const double vk = vb[b][k][lane];
+                const double val = corr ? fma(-cx1, c2, fma(-cx2, c1, vk)) : vk;
+                if (y < m) {
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
+                    b2 = b1;
+                    b1 = w;
+                    if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
+                } else if (y == m) {
+                    r2 = val;
+                } else {
+                    r1 = val;
+                }
+            }
+        }
+        // backward substitution (rows below m only; the lane re-reads what it stored above)
+        double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
+        issue(nb - 1, 0, true);
+        for (int j = 0; j < nb; ++j) {
+            const int bb = nb - 1 - j, b = j & 1, yb = bb * CH;
+            double tu[CH], tw[CH];
+#pragma unroll
+            for (int k = 0; k < CH; ++k) {
+                const bool in = yb + k < m;
+                tu[k] = in ? __ldg(du + yb + k) : 0.0;
+                tw[k] = in ? __ldg(dw + yb + k) : 0.0;
+            }
+            if (bb > 0) {
+                issue(bb - 1, b ^ 1, true);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+#pragma unroll
+            for (int k = CH - 1; k >= 0; --k) {
+                const int y = yb + k;
+                const double a_u = tu[k], a_w = tw[k];
+                if (y < m) {
+                    double w = fma(-a_u, f1, vb[b][k][lane]);
+                    w = fma(-a_w, f2, w);
+                    f2 = f1;
+                    f1 = w;
+                    if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
+                    if (y == m - 1) ym1 = w;
+                    if (y == m - 2) ym2 = w;
+                    if (y == 1) y1v = w;
+                    if (y == 0) y0v = w;
+                }
+            }
+        }
+        const double* om = tab + 7 * m;
+        const double a = om[4], b = om[5], d = om[6], e = om[7];
+        const double nx2 = r2 - (e * y0v + a * ym2 + b * ym1);
+        const double nx1 = r1 - (d * y0v + e * y1v + a * ym1);
+        const double x2 = om[0] * nx2 + om[1] * nx1;
+        const double x1 = om[2] * nx2 + om[3] * nx1;
+        // cNew = cBar + delta over cOld (cuPentCahnADI.cu:58-69, 89-100)
+        const double* cur = parity ? gd.buf[1] : gd.buf[0];
+        double* old = parity ? gd.buf[0] : gd.buf[1];
+        for (int yb = 0; yb < n; yb += UD) {
+            double i1[UD], i2[UD];
+#pragma unroll
+            for (int k = 0; k < UD; ++k) {
+                const bool in = yb + k < m;
+                i1[k] = in ? __ldg(inv1 + yb + k) : 0.0;
+                i2[k] = in ? __ldg(inv2 + yb + k) : 0.0;
+            }
+            double v[UD], cv[UD], ov[UD];
+#pragma unroll
+            for (int k = 0; k < UD; ++k) {
+                const size_t q = (size_t)(yb + k) * n + x;
+                v[k] = (yb + k < m) ? t[q] : 0.0;
+                cv[k] = cur[q];
+                ov[k] = old[q];
+            }
+#pragma unroll
+            for (int k = 0; k < UD; ++k) {
+                const int y = yb + k;
+                const double a1 = i1[k], a2 = i2[k];
+                double dlt;
+                if (y < m) dlt = fma(-a1, x2, fma(-a2, x1, v[k]));
+                else dlt = (y == m) ? x2 : x1;
+                const double cbar = fma(two, cv[k], -ov[k]);
+                if (in_bounds((long long)y * n + x, 0, (long long)n * n)) old[(size_t)y * n + x] = cbar + dlt;
+            }
+        }
+    }
+}
+
 ChConfig ch_config(int index) {
-    // {warps per right-hand-side CTA, y-sweep rows per batch, pipelined sweeps}
-    static const ChConfig tab[kChConfigs] = {{1, 32, 0}, {2, 32, 0}, {4, 32, 0}, {1, 16, 0}, {2, 16, 0},
-                                             {4, 16, 0}, {2, 16, 1}, {4, 16, 1}, {2, 32, 1}, {4, 32, 1}};
+    // {warps per right-hand-side CTA, y-sweep rows per batch, sweep kind, x-sweep columns per chunk (kinds 2, 3)}
+    static const ChConfig tab[kChConfigs] = {
+        {1, 32, 0, 16}, {2, 32, 0, 16}, {4, 32, 0, 16}, {1, 16, 0, 16}, {2, 16, 0, 16}, {4, 16, 0, 16},
+        {2, 16, 1, 16}, {4, 16, 1, 16}, {2, 32, 1, 16}, {4, 32, 1, 16}, {4, 16, 2, 16}, {4, 32, 2, 16},
+        {4, 8, 3, 16},  {4, 16, 3, 16}, {4, 8, 3, 8},   {4, 4, 3, 8},   {4, 4, 3, 16}};
     return tab[(index >= 0 && index < kChConfigs) ? index : 0];
+}
+
+void config_name(const ChConfig& c, char* name, size_t len) {
+    if (c.pipe >= 2)
+        snprintf(name, len, "rhs_warps%d_ychunk%d_pipe_regtab%s_xchunk%d", c.rhs_warps, c.y_chunk,
+                 c.pipe == 3 ? "_xy" : "", c.x_chunk);
+    else
+        snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
 }
 
 template <typename T>
@@ -742,10 +1049,20 @@ cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grid
     if (c.pipe) {
         // 64-100 registers and 8-17 KB of shared memory per one-warp CTA: up to 32 CTAs per SM
         const int gp = std::max(1, std::min(n_rows, sms * 32));
-        if (c.y_chunk == 32) ch_xsolve_pipe_kernel<32><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+        if (c.pipe >= 2 && c.x_chunk == 8)
+            ch_xsolve_pipe_rt_kernel<8><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+        else if (c.pipe >= 2)
+            ch_xsolve_pipe_rt_kernel<16><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+        else if (c.y_chunk == 32) ch_xsolve_pipe_kernel<32><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
         else ch_xsolve_pipe_kernel<16><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if (c.y_chunk == 32)
+        if (c.pipe == 3 && c.y_chunk == 4)
+            ch_ysolve_pipe_rt_kernel<4><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+        else if (c.pipe == 3 && c.y_chunk == 8)
+            ch_ysolve_pipe_rt_kernel<8><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+        else if (c.pipe == 3)
+            ch_ysolve_pipe_rt_kernel<16><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+        else if (c.y_chunk == 32)
             ch_ysolve_pipe_kernel<32><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
         else ch_ysolve_pipe_kernel<16><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
         return cudaGetLastError();
@@ -1317,7 +1634,7 @@ int custen_ch_batch_autotune(void* h, int steps, char* name, size_t len) {
     b->cfg = best;
     if (name && len) {
         const ChConfig c = ch_config(best);
-        snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
+        config_name(c, name, len);
     }
     return 0;
 }
@@ -1339,7 +1656,7 @@ int custen_ch_batch_config(void* h, char* name, size_t len) {
     Batch* b = static_cast<Batch*>(h);
     if (!b || !name || !len) return ch_fail_arg("invalid arguments");
     const ChConfig c = batch_config(b);
-    snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
+    config_name(c, name, len);
     return 0;
 }
 
