@@ -607,6 +607,32 @@ def run_gpu(args, world, rank, local):
         pg.destroy_process_group()
 
 
+def link_each_way_gbs(local: int, nbytes: int = 1 << 30, reps: int = 3) -> float:
+    """Host-link rate with both directions busy at once: a pinned host->device and a device->host copy of
+    nbytes each, on two streams, started together; nbytes / the time both take (best of reps). The
+    staged e2e path moves rows both ways at the same time, so this is its ceiling."""
+    import torch
+    dev = torch.device("cuda", local)
+    count = nbytes // 8
+    h_in = torch.ones(count, dtype=torch.float64, pin_memory=True)
+    h_out = torch.empty(count, dtype=torch.float64, pin_memory=True)
+    d_in = torch.empty(count, dtype=torch.float64, device=dev)
+    d_out = torch.ones(count, dtype=torch.float64, device=dev)
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    best = float("inf")
+    for _ in range(reps + 1):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        with torch.cuda.stream(s1):
+            d_in.copy_(h_in, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_out, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        best = min(best, time.perf_counter() - t0)
+    del h_in, h_out, d_in, d_out
+    return nbytes / best / 1e9
+
+
 def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
     """The same sweep through the reference-facing API on host buffers, numTiles=4, HOST offload,
     host<->device traffic inside the timed region.
@@ -649,6 +675,7 @@ def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
     for h in hs:
         h.compute(cs.HOST)
     cs._check(lib.custen_device_synchronize())
+    link = link_each_way_gbs(local) if kind == "pinned" else None
     h2d0, d2h0 = cs.transfer_bytes()
     launches0 = cs.kernel_launches()
     t0 = time.perf_counter()
@@ -666,10 +693,17 @@ def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
         (lib.custen_free_host if kind == "pinned" else lib.custen_free)(p)
     what = ("pinned host buffers, rows streamed through device staging slots in 32 MiB chunks"
             if kind == "pinned" else "managed buffers, tiles prefetched to the device and back (reference HOST path)")
-    return {"value": round(len(ops) * n * n / dt / 1e9, 3), "unit": "Gpts/s",
-            "h2d_bytes_per_step": (h2d1 - h2d0) // steps, "d2h_bytes_per_step": (d2h1 - d2h0) // steps,
-            "ms_per_step": round(dt * 1e3, 2), "steps": steps, "kernel_launches_per_step": launches,
-            "path": f"{n}^2, 12 operators, numTiles=4, Compute(HOST) per operator; {what}"}
+    out = {"value": round(len(ops) * n * n / dt / 1e9, 3), "unit": "Gpts/s",
+           "h2d_bytes_per_step": (h2d1 - h2d0) // steps, "d2h_bytes_per_step": (d2h1 - d2h0) // steps,
+           "ms_per_step": round(dt * 1e3, 2), "steps": steps, "kernel_launches_per_step": launches,
+           "path": f"{n}^2, 12 operators, numTiles=4, Compute(HOST) per operator; {what}"}
+    if link:
+        each_way = max(h2d1 - h2d0, d2h1 - d2h0) / steps / dt / 1e9
+        out["link"] = {"each_way_gbs": round(each_way, 1), "link_each_way_gbs": round(link, 1),
+                       "frac": round(each_way / link, 3),
+                       "note": "the host link measured just before, both directions busy at once (1 GiB each way); "
+                               "it varies from box to box"}
+    return out
 
 
 # ----------------------------------------------------------------------------------------------
