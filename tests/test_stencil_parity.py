@@ -381,3 +381,42 @@ def test_concurrent_handles_from_host_threads(gpu):
     for t in threads:
         t.join(timeout=300)
     assert not errors, errors
+
+
+def _random_cases(count: int, seed: int):
+    """Weighted-stencil geometries drawn within the reference's preconditions: nx % BLOCK_X == 0,
+    ny % numTiles == 0, (ny / numTiles) % BLOCK_Y == 0, L, R <= BLOCK_X, T, B <= BLOCK_Y, and at least two
+    blocks per direction (the non-periodic and y-periodic kernels assume it)."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    while len(cases) < count:
+        variant = int(rng.choice([cs.XP, cs.XNP, cs.YP, cs.YNP, cs.XYP, cs.XYNP]))
+        d = 0 if variant < 4 else (1 if variant < 8 else 2)
+        bx = int(rng.choice([8, 16, 32]))
+        by = int(rng.choice([4, 8, 16]))
+        tiles = int(rng.choice([1, 2, 3, 4]))
+        nx = bx * int(rng.integers(2, 9))
+        ny = by * tiles * int(rng.integers(2, 6))
+        L = R = T = B = 0
+        if d != 1:
+            L, R = int(rng.integers(0, min(4, bx) + 1)), int(rng.integers(0, min(4, bx) + 1))
+        if d != 0:
+            T, B = int(rng.integers(0, min(4, by) + 1)), int(rng.integers(0, min(4, by) + 1))
+        if L + R + T + B == 0:
+            continue
+        dtype = np.float64 if rng.random() < 0.7 else np.float32
+        config = int(rng.integers(0, cs.NUM_CONFIGS)) if rng.random() < 0.5 else None
+        cases.append((variant, nx, ny, tiles, bx, by, (L + R + 1, L, R, T + B + 1, T, B), dtype, config))
+    return cases
+
+
+@pytest.mark.parametrize("case", _random_cases(60, 2024), ids=lambda c: f"{cs.VARIANT_NAMES[c[0]]}-{c[1]}x{c[2]}-"
+                         f"t{c[3]}-b{c[4]}x{c[5]}-LRTB{c[6][1]}{c[6][2]}{c[6][4]}{c[6][5]}-"
+                         f"{'f64' if c[7] == np.float64 else 'f32'}-cfg{c[8]}")
+def test_parity_randomized(gpu, case):
+    """Random geometries within the reference's preconditions, bit-exact against the oracle on every
+    written point, sentinels kept on every untouched one."""
+    variant, nx, ny, tiles, bx, by, geom, dtype, config = case
+    got, ref, st, pre = run_both(variant, nx, ny, tiles, bx, by, geom, dtype=dtype, seed=nx + ny + tiles,
+                                 config=config)
+    check(got, ref, st, pre)
