@@ -23,6 +23,11 @@
 // Each kernel is persistent over a work list that covers all grids (largest first, claimed through
 // an atomic counter), so grids of different sizes share one launch. A step is three launches; pairs
 // of steps are captured in a CUDA graph.
+//
+// The sweeps come in three forms, all computing the same values (ChConfig, tuned per batch):
+// staged through registers (the kernels K2/K3 below), pipelined (the next chunk copied into shared
+// memory with cp.async while the current one runs), and pipelined with the chunk's table entries held
+// in registers by every lane (no per-element shuffles; the default, configuration 12).
 #include <cuda_runtime.h>
 
 #include <algorithm>
