@@ -571,7 +571,14 @@ def run_gpu(args, world, rank, local):
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, mean of the "
                                            "12 operators at 6144^2, scaled by the point count",
                          "peak_source": f"{hbm_src} hbm_gbs",
-                         "note": "16 B/pt algorithmic; FP64 kernels are bound by the FP64 FMA pipe, see fp64"},
+                         "note": "16 B/pt algorithmic; FP64 kernels are bound by the FP64 FMA pipe (binding): at "
+                                 "the measured FP64 FMA rate the sweep's operators cap at 1.4-2.5 TB/s",
+                         "binding": {"bound": "fp64", "achieved": round(achieved_fma / 1e9, 1),
+                                     "peak": round(fp64_rate / 1e9, 1), "unit": "G FMA/s",
+                                     "frac": round(achieved_fma / fp64_rate, 4),
+                                     "peak_source": "measured live (custen_probe_fma_rate)",
+                                     "hbm_frac_at_fp64_peak": round(achieved_gbs / hbm_peak * fp64_rate / achieved_fma,
+                                                                    4)}},
             "fp64": {"achieved_fma_s": round(achieved_fma / 1e9, 1), "peak_fma_s": round(fp64_rate / 1e9, 1),
                      "unit": "G FMA/s", "frac": round(achieved_fma / fp64_rate, 4),
                      "peak_source": "measured live (custen_probe_fma_rate)"},
