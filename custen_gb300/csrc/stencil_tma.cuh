@@ -172,21 +172,10 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
         const int s = it % S;
         const uint32_t parity = (uint32_t)((it / S) & 1);
         T* tile = ring + (size_t)s * stage_bytes / sizeof(T);
+        // Each thread waits on the stage itself (the wait acquires the copy's data for that thread), so
+        // no barrier is needed before reading it. A thread whose wait expired skips the tile's compute;
+        // the end-of-tile barrier then makes the exit decision uniform.
         const bool ok = mbar_wait(&full[s], parity);
-        if (__syncthreads_or(!ok)) {
-            // A copy never completed: record it, wait (bounded) for the copies this CTA still has in
-            // flight, and leave.
-            if (tid == 0) {
-                atomicOr(&g_custen_device_error, kErrMbarrierTimeout);
-                for (int k = 0; k < S; ++k) {
-                    const int tk = blockIdx.x + (it + k) * gridDim.x;
-                    if (tk >= tiles_total) break;
-                    mbar_wait(&full[(it + k) % S], (uint32_t)(((it + k) / S) & 1));
-                }
-            }
-            __syncthreads();
-            return;
-        }
         const int tyi = t / tiles_x, txi = t - tyi * tiles_x;
         const int x0 = txi * TW, y0 = tyi * TH;
         const bool rows_fix = (y0 == 0 && a.T > 0 && a.has_top) || (y0 + TH == a.rows && a.B > 0 && a.has_bot);
@@ -200,20 +189,35 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
             __syncthreads();
         }
         const bool all_write = tile_all_write(a, x0, x0 + TW, a.row0 + y0, a.row0 + y0 + TH);
-        if constexpr (MODE >= MODE_FIRST_SHAPE) {
-            using SH = typename ShapeOf<MODE>::type;
-            if (sizeof(T) == 4 || nlist == SH::H * SH::V)
-                compute_window_store<T, TW, TH, RPT, VEC, SH>(a, tile, coef_s, g, x0, y0, threadIdx.x,
-                                                              threadIdx.y, all_write);
-            else
+        if (ok) {
+            if constexpr (MODE >= MODE_FIRST_SHAPE) {
+                using SH = typename ShapeOf<MODE>::type;
+                if (sizeof(T) == 4 || nlist == SH::H * SH::V)
+                    compute_window_store<T, TW, TH, RPT, VEC, SH>(a, tile, coef_s, g, x0, y0, threadIdx.x,
+                                                                  threadIdx.y, all_write);
+                else
+                    compute_and_store<T, TW, TH, RPT, VEC>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0,
+                                                           threadIdx.x, threadIdx.y, false, all_write);
+            } else {
                 compute_and_store<T, TW, TH, RPT, VEC>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0,
-                                                       threadIdx.x, threadIdx.y, false, all_write);
-        } else {
-            compute_and_store<T, TW, TH, RPT, VEC>(a, tile, coef_s, list_off, list_w, nlist, g, x0, y0, threadIdx.x,
-                                                   threadIdx.y, is_fun, all_write);
+                                                       threadIdx.x, threadIdx.y, is_fun, all_write);
+            }
         }
         fence_proxy_async_smem();
-        __syncthreads();   // every thread is done with stage s
+        // every thread is done with stage s; a copy that never completed ends the CTA here: record it,
+        // wait (bounded) for the copies this CTA still has in flight, and leave
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(&g_custen_device_error, kErrMbarrierTimeout);
+                for (int k = 0; k < S; ++k) {
+                    const int tk = blockIdx.x + (it + k) * gridDim.x;
+                    if (tk >= tiles_total) break;
+                    mbar_wait(&full[(it + k) % S], (uint32_t)(((it + k) / S) & 1));
+                }
+            }
+            __syncthreads();
+            return;
+        }
         if (tid == 0) {
             const int tn = t + S * gridDim.x;
             if (tn < tiles_total) {
