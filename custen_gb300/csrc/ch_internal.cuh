@@ -16,6 +16,7 @@ struct GridDev {
     double* buf[2];       // the two field buffers: cCurr = buf[parity], cOld = buf[parity ^ 1]
     double* tmp;          // n x n work field (rhs, then the x-sweep solution)
     double* ends;         // 2 n values: the x sweep's last two unknowns of every row
+    double* hbuf;         // n x n h of the two-pass right-hand side (batch only; null elsewhere)
     const double* tab;    // solver table for n (layout below)
     int n;
     int pad;
@@ -48,15 +49,18 @@ struct ChConfig {
     int rhs_warps;
     int y_chunk;
     int pipe;
-    int x_chunk;   // columns per chunk of the register-table x sweep (pipe 2, 3): 8 or 16
+    int x_chunk;     // columns per chunk of the register-table x sweep (pipe 2, 3): 8 or 16
+    int rhs_split;   // 1: the right-hand side in two passes through GridDev::hbuf (batches only)
 };
-constexpr ChConfig kChDefault{4, 8, 3, 16};   // configuration 12, the fastest at 512 mixed grids
-constexpr int kChConfigs = 17;
+constexpr ChConfig kChDefault{4, 8, 3, 16, 0};   // configuration 12; needs no h buffer (server, one-grid step)
+constexpr int kChBatchDefault = 17;             // batches (they allocate the h buffer): two-pass right-hand side
+constexpr int kChConfigs = 19;
+constexpr int kChCounters = 4;   // work counters per step (zeroed before it)
 ChConfig ch_config(int index);   // 0 .. kChConfigs-1
 void config_name(const ChConfig& c, char* name, size_t len);
 
-// One step of every grid of a work list: right-hand side, x sweep, y sweep (3 launches on s).
-// counters: 3 zeroed work counters.
+// One step of every grid of a work list: right-hand side (one or two passes), x sweep, y sweep (3 or 4
+// launches on s). counters: kChCounters zeroed work counters.
 cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grids, const Item* items_rhs, int n_rhs,
                            const Item* items_rows, int n_rows, int parity, unsigned int* counters, int sms,
                            cudaStream_t s);

@@ -334,7 +334,7 @@ static int drop(Server* S, int id, const std::string& why, double now) {
 
 static int enqueue_steps(Server* S, int k) {
     for (int s = 0; s < k; ++s) {
-        SRV_TRY(cudaMemsetAsync(S->counters, 0, 3 * sizeof(unsigned int), S->stream), "Resetting counters");
+        SRV_TRY(cudaMemsetAsync(S->counters, 0, kChCounters * sizeof(unsigned int), S->stream), "Resetting counters");
         SRV_TRY(launch_ch_step(kChDefault, S->rhs_fp32 != 0, S->grids_d, S->items_rhs_d, S->n_rhs, S->items_rows_d,
                                S->n_rows, S->parity, S->counters, S->sms, S->stream),
                 "Launching a step");
@@ -468,7 +468,7 @@ int custen_ch_server_create(void** out, double hbm_budget_bytes, int rhs_dtype, 
     S->chunk = chunk_steps;
     S->keep_results = keep_results;
     cudaError_t e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMallocAsync(&S->counters, 4 * sizeof(unsigned int), S->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&S->counters, kChCounters * sizeof(unsigned int), S->stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&S->mass_d, sizeof(double), S->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
     if (e != cudaSuccess) {

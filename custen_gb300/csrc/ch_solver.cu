@@ -137,6 +137,117 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
 }
 
 // ------------------------------------------------------------------------------------------------
+// K1 in two passes (batch configurations with rhs_split): h is formed once per point and kept in the
+// grid's h buffer, so that no block recomputes its neighbours' halo values of h (K1 above forms cBar
+// on a 2-point halo and h on a 1-point halo of every block: about 16.3 FP64 operations per point;
+// the two passes take about 15.1). The expressions and their order are those of K1, so the results
+// are the same bit for bit.
+// ------------------------------------------------------------------------------------------------
+// Pass 1: h = sigma_nl * (c^3 - c) - sigma_lin * Lap(cBar), cBar over the block and a 1-point halo.
+template <typename T, int NW>
+__global__ void __launch_bounds__(NW * BLK) ch_h_kernel(const GridDev* __restrict__ grids,
+                                                        const Item* __restrict__ items, int n_items, int parity,
+                                                        unsigned int* counter) {
+    __shared__ T cb[34][35];
+    __shared__ T gg[32][33];   // sigma_nl * (c^3 - c)
+    __shared__ int s_item;
+    constexpr int NT = NW * BLK;
+    const int tid = threadIdx.x;
+    const volatile double* factors = g_rhs_factors;
+    const T two = (T)factors[0], m_four = (T)factors[1];
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* cur = parity ? gd.buf[1] : gd.buf[0];
+        const double* old = parity ? gd.buf[0] : gd.buf[1];
+        const double* tab = gd.tab;
+        const int bpr = n / BLK;
+        const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
+        const T s_lin = (T)(-tab[7 * m + 8 + 2]);
+        const T s_nl = (T)tab[7 * m + 33 + 1];
+#pragma unroll 4
+        for (int e = tid; e < 34 * 34; e += NT) {
+            const int r = e / 34, c = e - r * 34;
+            int gy = y0 - 1 + r, gx = x0 - 1 + c;
+            gy = gy < 0 ? gy + n : (gy >= n ? gy - n : gy);
+            gx = gx < 0 ? gx + n : (gx >= n ? gx - n : gx);
+            const double cv = cur[(size_t)gy * n + gx];
+            const double ov = old[(size_t)gy * n + gx];
+            const T c32 = (T)cv, o32 = (T)ov;
+            cb[r][c] = fma(two, c32, -o32);
+            if (r >= 1 && r < 33 && c >= 1 && c < 33) gg[r - 1][c - 1] = s_nl * fma(c32 * c32, c32, -c32);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int e = tid; e < 32 * 32; e += NT) {
+            const int r = e / 32, c = e - r * 32;
+            const T lap = fma(m_four, cb[r + 1][c + 1], (cb[r][c + 1] + cb[r + 2][c + 1]) + (cb[r + 1][c] + cb[r + 1][c + 2]));
+            const long long q = (long long)(y0 + r) * n + x0 + c;
+            if (in_bounds(q, 0, (long long)n * n)) gd.hbuf[q] = (double)fma(-s_lin, lap, gg[r][c]);
+        }
+        __syncthreads();
+    }
+}
+
+// Pass 2: rhs = Lap(h) - (2/3)(cCurr - cOld) (findRHS, cuPentCahnADI.cu:72-86), h over the block and a
+// 1-point halo from the h buffer.
+template <typename T, int NW>
+__global__ void __launch_bounds__(NW * BLK) ch_rhs2_kernel(const GridDev* __restrict__ grids,
+                                                           const Item* __restrict__ items, int n_items, int parity,
+                                                           unsigned int* counter) {
+    __shared__ T hh[34][35];
+    __shared__ T dco[32][33];
+    __shared__ int s_item;
+    constexpr int NT = NW * BLK;
+    const int tid = threadIdx.x;
+    const int lane = tid & (BLK - 1), warp = tid / BLK;
+    const volatile double* factors = g_rhs_factors;
+    const T m_four = (T)factors[1], m_two_thirds = (T)factors[2];
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n;
+        const double* cur = parity ? gd.buf[1] : gd.buf[0];
+        const double* old = parity ? gd.buf[0] : gd.buf[1];
+        const int bpr = n / BLK;
+        const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
+#pragma unroll 4
+        for (int e = tid; e < 34 * 34; e += NT) {
+            const int r = e / 34, c = e - r * 34;
+            int gy = y0 - 1 + r, gx = x0 - 1 + c;
+            gy = gy < 0 ? gy + n : (gy >= n ? gy - n : gy);
+            gx = gx < 0 ? gx + n : (gx >= n ? gx - n : gx);
+            hh[r][c] = (T)gd.hbuf[(size_t)gy * n + gx];
+            if (r >= 1 && r < 33 && c >= 1 && c < 33) {
+                const T c32 = (T)cur[(size_t)gy * n + gx], o32 = (T)old[(size_t)gy * n + gx];
+                dco[r - 1][c - 1] = c32 - o32;
+            }
+        }
+        __syncthreads();
+        const int j = lane;
+        double* out = gd.tmp + (size_t)y0 * n + x0 + j;
+#pragma unroll 4
+        for (int rr = warp; rr < BLK; rr += NW) {
+            const T lap = fma(m_four, hh[rr + 1][j + 1], (hh[rr][j + 1] + hh[rr + 2][j + 1]) + (hh[rr + 1][j] + hh[rr + 1][j + 2]));
+            if (!in_bounds((long long)(y0 + rr) * n + x0 + j, 0, (long long)n * n)) continue;
+            out[(size_t)rr * n] = (double)fma(m_two_thirds, dco[rr][j], lap);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
 // K2: x sweep (lane = row), 32-column chunks through shared memory
 // ------------------------------------------------------------------------------------------------
 // The recurrences are latency chains of FP64 operations; everything else is taken off their path:
@@ -1015,20 +1126,35 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_pipe_rt_kernel(const GridDev* _
 }
 
 ChConfig ch_config(int index) {
-    // {warps per right-hand-side CTA, y-sweep rows per batch, sweep kind, x-sweep columns per chunk (kinds 2, 3)}
+    // {warps per right-hand-side CTA, y-sweep rows per batch, sweep kind, x-sweep columns per chunk (kinds 2,
+    // 3), two-pass right-hand side}
     static const ChConfig tab[kChConfigs] = {
         {1, 32, 0, 16}, {2, 32, 0, 16}, {4, 32, 0, 16}, {1, 16, 0, 16}, {2, 16, 0, 16}, {4, 16, 0, 16},
         {2, 16, 1, 16}, {4, 16, 1, 16}, {2, 32, 1, 16}, {4, 32, 1, 16}, {4, 16, 2, 16}, {4, 32, 2, 16},
-        {4, 8, 3, 16},  {4, 16, 3, 16}, {4, 8, 3, 8},   {4, 4, 3, 8},   {4, 4, 3, 16}};
+        {4, 8, 3, 16},  {4, 16, 3, 16}, {4, 8, 3, 8},   {4, 4, 3, 8},   {4, 4, 3, 16},
+        {4, 8, 3, 16, 1}, {2, 8, 3, 16, 1}};
     return tab[(index >= 0 && index < kChConfigs) ? index : 0];
 }
 
 void config_name(const ChConfig& c, char* name, size_t len) {
     if (c.pipe >= 2)
-        snprintf(name, len, "rhs_warps%d_ychunk%d_pipe_regtab%s_xchunk%d", c.rhs_warps, c.y_chunk,
-                 c.pipe == 3 ? "_xy" : "", c.x_chunk);
+        snprintf(name, len, "rhs_warps%d%s_ychunk%d_pipe_regtab%s_xchunk%d", c.rhs_warps, c.rhs_split ? "_2pass" : "",
+                 c.y_chunk, c.pipe == 3 ? "_xy" : "", c.x_chunk);
     else
         snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
+}
+
+// the two passes of the split right-hand side; pass 2 claims work through the step's fourth counter
+template <typename T>
+static void launch_rhs2(int nw, int grid, const GridDev* g, const Item* it, int n, int parity, unsigned int* ctr,
+                        cudaStream_t s) {
+    if (nw == 4) {
+        ch_h_kernel<T, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr);
+        ch_rhs2_kernel<T, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
+    } else {
+        ch_h_kernel<T, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr);
+        ch_rhs2_kernel<T, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
+    }
 }
 
 template <typename T>
@@ -1047,8 +1173,14 @@ cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grid
     // persistent grids over the work lists; CTAs beyond the resident ones find the lists empty
     const int g1 = std::max(1, std::min(n_rhs, sms * 32 / c.rhs_warps));
     const int g23 = std::max(1, std::min(n_rows, sms * 16));
-    if (rhs_fp32) launch_rhs<float>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
-    else launch_rhs<double>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+    if (c.rhs_split) {
+        if (rhs_fp32) launch_rhs2<float>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+        else launch_rhs2<double>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+    } else if (rhs_fp32) {
+        launch_rhs<float>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+    } else {
+        launch_rhs<double>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (c.pipe) {
@@ -1211,11 +1343,11 @@ struct Batch {
     bool own_stream = false;
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};   // pair of steps starting at parity 0 / 1
     int sms = 0;
-    int cfg = -1;   // ch_config index; -1: kChDefault
+    int cfg = -1;   // ch_config index; -1: kChBatchDefault
     unsigned long long launches = 0;
 };
 
-static ChConfig batch_config(const Batch* b) { return b->cfg < 0 ? kChDefault : ch_config(b->cfg); }
+static ChConfig batch_config(const Batch* b) { return ch_config(b->cfg < 0 ? kChBatchDefault : b->cfg); }
 
 static thread_local std::string g_ch_err;
 static int ch_fail(cudaError_t e, const char* what) {
@@ -1234,8 +1366,8 @@ static int ch_fail_arg(const std::string& msg) {
     } while (0)
 
 static int enqueue_step(Batch* b, int parity, int slot) {
-    unsigned int* ctr = b->counters + 3 * slot;
-    CH_TRY(cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned int), b->stream), "Resetting work counters");
+    unsigned int* ctr = b->counters + kChCounters * slot;
+    CH_TRY(cudaMemsetAsync(ctr, 0, kChCounters * sizeof(unsigned int), b->stream), "Resetting work counters");
     CH_TRY(launch_ch_step(batch_config(b), b->rhs_fp32 != 0, b->grids_d, b->items_rhs, b->n_items_rhs, b->items_rows,
                           b->n_items_rows, parity, ctr, b->sms, b->stream),
            "Launching a step");
@@ -1281,7 +1413,7 @@ constexpr int kNoAllocRows = kNoAllocMaxN / BLK;
 constexpr size_t kNoAllocRhsOff = align256(kNoAllocGridOff + sizeof(GridDev));
 constexpr size_t kNoAllocRowsOff = align256(kNoAllocRhsOff + sizeof(Item) * kNoAllocBlocks);
 constexpr size_t kNoAllocCtrOff = align256(kNoAllocRowsOff + sizeof(Item) * kNoAllocRows);
-constexpr size_t kNoAllocBytes = align256(kNoAllocCtrOff + 4 * sizeof(unsigned int));
+constexpr size_t kNoAllocBytes = align256(kNoAllocCtrOff + kChCounters * sizeof(unsigned int));
 
 static __device__ __align__(256) unsigned char g_ch_noalloc_scratch[kNoAllocBytes];
 
@@ -1341,12 +1473,12 @@ int custen_ch_batch_create(void** out, int nsims, const int* n, const double* lx
         }
         GridDev g{};
         const size_t bytes = (size_t)ns * ns * sizeof(double);
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 5; ++k) {   // cCurr / cOld, tmp, row ends, h of the two-pass right-hand side
             double* p = nullptr;
-            cudaError_t e = cudaMalloc(&p, k < 3 ? bytes : 2 * ns * sizeof(double));
+            cudaError_t e = cudaMalloc(&p, k == 3 ? 2 * ns * sizeof(double) : bytes);
             if (e != cudaSuccess) return cleanup_fail(ch_fail(e, "Allocating grid fields"));
             b->allocs.push_back(p);
-            if (k < 2) g.buf[k] = p; else if (k == 2) g.tmp = p; else g.ends = p;
+            if (k < 2) g.buf[k] = p; else if (k == 2) g.tmp = p; else if (k == 3) g.ends = p; else g.hbuf = p;
         }
         g.tab = tab;
         g.n = ns;
@@ -1371,7 +1503,7 @@ int custen_ch_batch_create(void** out, int nsims, const int* n, const double* lx
     if (e == cudaSuccess) e = cudaMalloc(&b->items_rows, rows.size() * sizeof(Item));
     if (e == cudaSuccess)
         e = cudaMemcpy(b->items_rows, rows.data(), rows.size() * sizeof(Item), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&b->counters, 6 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->counters, 2 * kChCounters * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&b->mass_d, sizeof(double));
     if (e != cudaSuccess) return cleanup_fail(ch_fail(e, "Allocating work lists"));
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
@@ -1455,12 +1587,13 @@ int custen_ch_batch_step(void* h, int steps, int use_graph) {
     if (!b || steps < 0) return ch_fail_arg("invalid arguments");
     cudaSetDevice(b->device);
     int left = steps;
+    const int per_step = 3 + batch_config(b).rhs_split;   // kernel launches in one step
     if (use_graph && left >= 2) {
         int st = capture_pairs(b);
         if (st) return st;
         while (left >= 2) {
             CH_TRY(cudaGraphLaunch(b->graph_exec[b->parity], b->stream), "Launching step graph");
-            b->launches += 6;
+            b->launches += 2 * per_step;
             left -= 2;
             b->steps_done += 2;
         }
@@ -1468,7 +1601,7 @@ int custen_ch_batch_step(void* h, int steps, int use_graph) {
     while (left > 0) {
         int st = enqueue_step(b, b->parity, 0);
         if (st) return st;
-        b->launches += 3;
+        b->launches += per_step;
         b->parity ^= 1;
         --left;
         ++b->steps_done;
@@ -1555,7 +1688,7 @@ int custen_ch_step_noalloc(const double* c_old, const double* c_cur, double* c_n
            "Uploading the work list");
     // the work counters must start at zero on every call (the array keeps the previous call's values)
     unsigned int* ctr = reinterpret_cast<unsigned int*>(base + kNoAllocCtrOff);
-    CH_TRY(cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned int), s), "Clearing the work counters");
+    CH_TRY(cudaMemsetAsync(ctr, 0, kChCounters * sizeof(unsigned int), s), "Clearing the work counters");
     const GridDev* gd = reinterpret_cast<const GridDev*>(base + kNoAllocGridOff);
     const Item* it_rhs = reinterpret_cast<const Item*>(base + kNoAllocRhsOff);
     const Item* it_rows = reinterpret_cast<const Item*>(base + kNoAllocRowsOff);

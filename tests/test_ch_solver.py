@@ -111,7 +111,7 @@ def test_fp32_stencil_variant_error_reported(gpu):
     b.close()
 
 
-CH_CONFIGS = 17
+CH_CONFIGS = 19
 
 
 def test_every_kernel_configuration_gives_identical_fields(gpu):
