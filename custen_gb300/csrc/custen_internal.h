@@ -62,6 +62,10 @@ struct StencilArgs {
 };
 
 // Write rule of the reference for point (x, gy) of the field, gy a field row.
+// Division-free: only a tile's first and last block rows and the field's first and last block columns
+// have rules, so "first block" is x < bx, "last block" is x >= nx - bx (nx is a multiple of bx), and the
+// position inside such a block follows by subtraction; the tile of row gy is found by stepping over
+// the (few) tiles. The edge tiles of a launch evaluate this per point.
 __host__ __device__ inline int point_action(int variant, int x, int gy, int nx, int L, int R, int T, int B,
                                             int bx, int by, int nyTile, int numTiles) {
     switch (variant) {
@@ -76,36 +80,43 @@ __host__ __device__ inline int point_action(int variant, int x, int gy, int nx, 
         // skipped in the last block (:165-170).
         if (x < L || x >= nx - R) return ACT_SKIP;
         return ACT_WRITE;
+    default:
+        break;
+    }
+    int t = 0, yt = gy;   // tile of row gy and the row inside it
+    while (yt >= nyTile && t < numTiles - 1) {
+        yt -= nyTile;
+        ++t;
+    }
+    switch (variant) {
     case V_YNP:
-    case V_YNPFUN: {
+    case V_YNPFUN:
         // kernel2DYnp / kernel2DYnpFun: in the first tile block row 0 stores rows T..BY-1 only
         // (2d_y_np_kernel.cu:167-192, 2d_y_np_fun_kernel.cu:173-193); in the last tile the last block
         // row stores ty < BY - B (2d_y_np_kernel.cu:246-249, 2d_y_np_fun_kernel.cu:242).
-        int t = gy / nyTile, yt = gy - t * nyTile;
         if (t == 0 && yt < T) return ACT_SKIP;
         if (t == numTiles - 1 && yt >= nyTile - B) return ACT_SKIP;
         return ACT_WRITE;
-    }
     case V_XYNP:
     case V_XYNPFUN: {
         // kernel2DXYnp: nine block cases tested in this order (2d_xy_np_kernel.cu:136-958).
-        int t = gy / nyTile, yt = gy - t * nyTile;
-        int bxi = x / bx, tx = x - bxi * bx, nbx = nx / bx;
-        int byi = yt / by, ty = yt - byi * by, nby = nyTile / by;
-        bool tileTop = (t == 0), tileBottom = (t == numTiles - 1);
-        bool left = (bxi == 0), right = (bxi == nbx - 1), topb = (byi == 0), botb = (byi == nby - 1);
+        const bool left = x < bx, right = x >= nx - bx;             // first / last block column
+        const bool topb = yt < by, botb = yt >= nyTile - by;        // first / last block row of the tile
+        const int txl = x, txr = x - (nx - bx);                     // tx inside the first / last block
+        const int tyt = yt, tyb = yt - (nyTile - by);               // ty inside the first / last block row
+        const bool tileTop = (t == 0), tileBottom = (t == numTiles - 1);
         bool ok;
-        if (left && topb) ok = tileTop ? (tx >= L && ty >= T) : (tx >= L);                      // :208-219
-        else if (right && topb) ok = tileTop ? (tx < bx - R && ty >= T) : (tx < bx - R);        // :301-312
-        else if (left && botb) ok = tileBottom ? (tx >= L && ty < by - B) : (tx >= L);          // :393-404
-        else if (right && botb) ok = tileBottom ? (tx < bx - R && ty < by - B) : (tx < bx - R); // :484-495
-        else if (topb) ok = tileTop ? (ty >= T) : true;                                         // :593-602
-        else if (botb) ok = tileBottom ? (ty < by - B) : true;                                  // :699-708
-        else if (left) ok = (tx >= L);                                                          // :784
+        if (left && topb) ok = tileTop ? (txl >= L && tyt >= T) : (txl >= L);                     // :208-219
+        else if (right && topb) ok = tileTop ? (txr < bx - R && tyt >= T) : (txr < bx - R);       // :301-312
+        else if (left && botb) ok = tileBottom ? (txl >= L && tyb < by - B) : (txl >= L);         // :393-404
+        else if (right && botb) ok = tileBottom ? (txr < bx - R && tyb < by - B) : (txr < bx - R); // :484-495
+        else if (topb) ok = tileTop ? (tyt >= T) : true;                                        // :593-602
+        else if (botb) ok = tileBottom ? (tyb < by - B) : true;                                 // :699-708
+        else if (left) ok = (txl >= L);                                                         // :784
         // Right edge, middle block rows: the reference guard is tx < BX - L (:862; :787 for Fun).
         // When L < R the reference stores values read from shared memory it never loaded for
         // tx in [BX-R, BX-L); those points are left untouched here.
-        else if (right) ok = (tx < bx - L) && (tx < bx - R);
+        else if (right) ok = (txr < bx - L) && (txr < bx - R);
         else ok = true;
         return ok ? ACT_WRITE : ACT_SKIP;
     }
