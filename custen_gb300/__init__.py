@@ -29,7 +29,7 @@ XYWENOADVP = 12   # WENO5 advection, periodic (WenoAdvection)
 F64, F32 = 0, 1
 DEVICE, HOST = 0, 1
 HANDLE_BYTES = 200
-NUM_CONFIGS = 5   # kernel configurations per element type (stencil_configs.h)
+NUM_CONFIGS = 6   # kernel configurations per element type (stencil_configs.h)
 
 _lib = None
 

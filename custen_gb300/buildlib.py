@@ -35,7 +35,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-rdc=true", "-Xcompiler", "-fPI
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 
 # stencil_cfg.cu is compiled once per entry of the configuration table (stencil_configs.h).
-NUM_CONFIGS = 5
+NUM_CONFIGS = 6
 CFG_UNITS = [(f"stencil_cfg_{d}_{k}", "stencil_cfg.cu", [f"-DCUSTEN_CFG_DTYPE={d}", f"-DCUSTEN_CFG_INDEX={k}"])
              for d in (0, 1) for k in range(NUM_CONFIGS)]
 # Translation units of the static drop-in library (the reference's libcuSten.a surface):

@@ -22,13 +22,14 @@ struct StencilConfig {
     int tw, th, rpt, vec;
 };
 
-constexpr int kNumConfigs = 5;
+constexpr int kNumConfigs = 6;
 constexpr StencilConfig kConfigsF64[kNumConfigs] = {
     {64, 32, 4, 2},    // 32 x 8 threads, 2 x 4 outputs each (16-byte vectors)
     {32, 32, 4, 2},    // 16 x 8: twice the tiles, for small fields
     {64, 16, 2, 2},    // 32 x 8, shallow register window
     {64, 32, 4, 1},    // 64 x 8, 8-byte accesses
     {64, 64, 8, 2},    // 32 x 8, deep register window
+    {32, 16, 2, 2},    // 16 x 8: four times the tiles, for the smallest fields
 };
 constexpr StencilConfig kConfigsF32[kNumConfigs] = {
     {128, 32, 4, 4},   // 32 x 8 threads, 4 x 4 outputs each (16-byte vectors)
@@ -36,6 +37,7 @@ constexpr StencilConfig kConfigsF32[kNumConfigs] = {
     {128, 16, 2, 4},   // 32 x 8, shallow register window
     {128, 32, 4, 2},   // 64 x 8, 8-byte accesses
     {128, 64, 8, 4},   // 32 x 8, deep register window
+    {64, 16, 2, 4},    // 16 x 8: four times the tiles, for the smallest fields
 };
 
 // One launch with configuration `cfg` (0 .. kNumConfigs-1) of element type `dtype`; *path = 1 when
