@@ -461,9 +461,9 @@ def run_gpu(args, world, rank, local):
                    "fp64_frac": round(dfma_pt * n * n / (ms * 1e-3) / fp64_rate, 3)}
 
     # ---- e2e: reference-facing API with host buffers (numTiles=4, HOST offload) ----
-    # Run before the WENO and pentadiagonal legs: measured after them (they build multi-GiB host arrays
-    # for their inputs), the same staged e2e reached 0.5-0.8 of the host link instead of 0.9 on the same
-    # box, with the link itself unchanged.
+    # The e2e legs run early, before the legs that build multi-GiB host arrays. The staged e2e reaches
+    # 0.5-0.9 of the host link measured alongside it, from one process to the next, with every host
+    # buffer copying at full rate on its own (e2e.link carries both measurements).
     e2e = e2e_managed = None
     if not args.skip_e2e:
         e2e = run_e2e(args, cs, np, local, ops, "pinned")
@@ -686,6 +686,7 @@ def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
         h.compute(cs.HOST)
     cs._check(lib.custen_device_synchronize())
     link = link_each_way_gbs(local) if kind == "pinned" else None
+    per_buffer = host_buffer_rates(lib, local, [inp] + outs, nbytes) if kind == "pinned" else None
     h2d0, d2h0 = cs.transfer_bytes()
     launches0 = cs.kernel_launches()
     t0 = time.perf_counter()
@@ -710,9 +711,37 @@ def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
     if link:
         each_way = max(h2d1 - h2d0, d2h1 - d2h0) / steps / dt / 1e9
         out["link"] = {"each_way_gbs": round(each_way, 1), "link_each_way_gbs": round(link, 1),
-                       "frac": round(each_way / link, 3),
+                       "frac": round(each_way / link, 3), "host_buffers": per_buffer,
                        "note": "the host link measured just before, both directions busy at once (1 GiB each way); "
-                               "it varies from box to box"}
+                               "host_buffers: one-way copy rates of every host buffer of this leg"}
+    return out
+
+
+def host_buffer_rates(lib, local, ptrs, nbytes, probe=1 << 28):
+    """One-way copy rate of pinned host buffers of nbytes each (host->device and device->host, the first
+    min(probe, nbytes) bytes of each): the slowest and the median. A buffer whose pages sit far from
+    the GPU shows here."""
+    import ctypes
+    import torch
+    probe = min(probe, nbytes)   # never past the end of a buffer
+    dev = torch.device("cuda", local)
+    d = torch.empty(probe // 8, dtype=torch.float64, device=dev)
+    rates = {"h2d": [], "d2h": []}
+    for p in ptrs:
+        for direction in ("h2d", "d2h"):
+            src, dst = (p, d.data_ptr()) if direction == "h2d" else (d.data_ptr(), p)
+            lib.custen_memcpy(ctypes.c_void_p(dst), ctypes.c_void_p(src), probe)   # warm
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            lib.custen_memcpy(ctypes.c_void_p(dst), ctypes.c_void_p(src), probe)
+            torch.cuda.synchronize(dev)
+            rates[direction].append(probe / (time.perf_counter() - t0) / 1e9)
+    del d
+    out = {}
+    for direction, r in rates.items():
+        if r:
+            r.sort()
+            out[direction] = {"min_gbs": round(r[0], 1), "median_gbs": round(r[len(r) // 2], 1), "buffers": len(r)}
     return out
 
 
