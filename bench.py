@@ -428,7 +428,9 @@ def run_gpu(args, world, rank, local):
         torch.cuda.synchronize(dev)
         launches = cs.kernel_launches() - launches0
         total_ms = t0.elapsed_time(t1)
-        per_op = [sum(ev[s][k][0].elapsed_time(ev[s][k][1]) for s in range(steps)) / steps for k in range(len(hs))]
+        # per operator: the median of its timed Computes
+        per_op = [sorted(ev[s][k][0].elapsed_time(ev[s][k][1]) for s in range(steps))[steps // 2]
+                  for k in range(len(hs))]
         return total_ms, per_op, launches
 
     # ---- FP64 sweep (headline) ----
@@ -490,8 +492,9 @@ def run_gpu(args, world, rank, local):
                                 "pointer, as a user-defined function does"}
 
     # ---- FP32 precision variant: same sweep in FP32, error against the FP64 outputs ----
-    fp32 = None
+    fp32 = fp32_small = None
     if not args.skip_fp32:
+        fp32_small = run_precision(cs, torch, dev, 4096)
         inp32, outs32, hs32, keep32 = build_handles(torch.float32, cs.F32)
         ms32, per32, _ = timed_sweep(hs32, max(1, args.steps), 3)
         fp32 = {"gpts_s": round(pts_step / (ms32 / max(1, args.steps) * 1e-3) / 1e9, 3),
@@ -591,6 +594,8 @@ def run_gpu(args, world, rank, local):
         }
         if fp32 is not None:
             line["fp32"] = fp32
+        if fp32_small is not None:
+            line["fp32_4096"] = fp32_small
         if e2e is not None:
             line["e2e"] = e2e
         if e2e_managed is not None:
@@ -835,6 +840,50 @@ def event_ms(torch, fn, reps=5):
     return sorted(times)[len(times) // 2]
 
 
+def run_precision(cs, torch, dev, n, steps=20):
+    """The precision variant at a second size (n^2, device-resident, numTiles 1): every stencil in FP64 and
+    in FP32 on the same input (cast from FP64), the FP32 error against the FP64 output (max abs, rel L2)
+    and the achieved GB/s of both (median of `steps` timed Computes)."""
+    x = torch.arange(n, device=dev, dtype=torch.float64) * (2 * math.pi / n)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    f64 = (torch.sin(3 * x)[None, :] * torch.cos(5 * x)[:, None]
+           + (torch.rand((n, n), device=dev, dtype=torch.float64, generator=g) * 2e-3 - 1e-3)).contiguous()
+    f32 = f64.float().contiguous()
+    s = torch.cuda.current_stream(dev)
+    per = {}
+    for (nm, v, H, L, R, V, T, B, w, fun, _) in operators(n):
+        res = {}
+        for dt_t, cdt, f in ((torch.float64, cs.F64, f64), (torch.float32, cs.F32, f32)):
+            wt = torch.tensor(w, device=dev, dtype=dt_t)
+            o = torch.zeros((n, n), device=dev, dtype=dt_t)
+            func = cs.builtin_function(fun, cdt) if fun >= 0 else None
+            h = cs.Stencil(v, n, n, o, f, wt, H=H, L=L, R=R, V=V, T=T, B=B, block_x=32, block_y=8, dtype=cdt,
+                           ncoef=len(w), func=func)
+            for _ in range(3):
+                h.compute(stream=s)
+            times = []
+            for _ in range(steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                h.compute(stream=s)
+                e1.record(s)
+                torch.cuda.synchronize(dev)
+                times.append(e0.elapsed_time(e1))
+            h.destroy()
+            res[cdt] = (o, sorted(times)[steps // 2], wt)
+        d = res[cs.F32][0].double() - res[cs.F64][0]
+        per[nm] = {"fp32_gbs": round(8.0 * n * n / (res[cs.F32][1] * 1e-3) / 1e9, 1),
+                   "fp64_gbs": round(16.0 * n * n / (res[cs.F64][1] * 1e-3) / 1e9, 1),
+                   "max_abs_err": float(d.abs().max().item()),
+                   "rel_l2": float((d.norm() / res[cs.F64][0].norm()).item())}
+    del f64, f32
+    torch.cuda.empty_cache()
+    return {"n": n, "per_op": per,
+            "note": "fields of 134 MB (FP64, about the size of L2) and 67 MB (FP32, inside L2): the GB/s here "
+                    "are not HBM figures"}
+
+
 def run_pent(cs, torch, dev, hbm_peak, m=256, batch=1 << 18):
     """cuPentBatch's factorisation and solve over `batch` interleaved systems of m unknowns (the layout's
     wire format), and the inverted-pivot solve; 72 B per row of compulsory traffic in each."""
@@ -1013,7 +1062,7 @@ def run_ch_served(args, cs):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=16384)
