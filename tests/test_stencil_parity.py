@@ -420,3 +420,47 @@ def test_parity_randomized(gpu, case):
     got, ref, st, pre = run_both(variant, nx, ny, tiles, bx, by, geom, dtype=dtype, seed=nx + ny + tiles,
                                  config=config)
     check(got, ref, st, pre)
+
+
+@pytest.mark.parametrize("variant", [cs.XYP, cs.YNP])
+def test_field_beyond_2gib(gpu, variant):
+    """A 16384 x 20480 FP64 field (2.68 GB, element offsets past 2^31 bytes) with small-integer inputs and
+    integer weights: every partial sum is exact in FP64, so the result does not depend on summation order
+    and plain numpy sums give it bit for bit. Checked on row bands at both ends (periodic wrap across
+    them) and around the 2^31-byte offset."""
+    import torch
+    nx, ny = 16384, 20480
+    H, L, R, V, T, B = 5, 2, 2, 5, 2, 2
+    if variant == cs.YNP:
+        H, L, R = 1, 0, 0
+    w = np.random.default_rng(4).integers(-3, 4, H * V).astype(np.float64)
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    inp = torch.randint(0, 16, (ny, nx), device=dev, generator=g).double()
+    out = torch.full((ny, nx), -1.0, device=dev, dtype=torch.float64)
+    wt = torch.tensor(w, device=dev)
+    s = cs.Stencil(variant, nx, ny, out.data_ptr(), inp.data_ptr(), wt.data_ptr(), H=H, L=L, R=R, V=V, T=T, B=B,
+                   block_x=32, block_y=8)
+    s.compute()
+    torch.cuda.synchronize(dev)
+    s.destroy()
+    row_2gib = (1 << 31) // (8 * nx)   # first row past the 2^31-byte offset
+    bands = [(0, 40), (row_2gib - 20, row_2gib + 20), (ny - 40, ny)]
+    for r0, r1 in bands:
+        rows = np.arange(r0 - T, r1 + B) % ny
+        window = inp[torch.as_tensor(rows, device=dev)].cpu().numpy()
+        ref = np.zeros((r1 - r0, nx))
+        for j in range(V):
+            for i in range(H):
+                ref += w[j * H + i] * np.roll(window[j:j + r1 - r0], -(i - L), axis=1)
+        got = out[r0:r1].cpu().numpy()
+        if variant == cs.YNP:
+            # Ynp leaves the field's first T and last B rows untouched (numTiles 1)
+            keep = np.ones(r1 - r0, dtype=bool)
+            keep[(np.arange(r0, r1) < T) | (np.arange(r0, r1) >= ny - B)] = False
+            assert np.all(got[~keep] == -1.0)
+            got, ref = got[keep], ref[keep]
+        assert np.array_equal(got, ref), f"rows {r0}..{r1}"
+    del inp, out
+    torch.cuda.empty_cache()
