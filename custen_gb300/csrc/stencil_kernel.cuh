@@ -44,6 +44,14 @@ struct TileGeom {
         SR = TH + a.T + a.B;
     }
     __host__ __device__ size_t tile_bytes() const { return (size_t)SR * SW * sizeof(T); }
+    // TMA path, periodic in x: per stage, the side areas that the wrap-around boxes fill (LP x SR and
+    // RP x SR elements, each rounded up to 128 bytes); zero when the launch does not wrap.
+    __host__ __device__ int wrap_l_bytes(const StencilArgs& a) const {
+        return a.wrap_x && LP > 0 ? round_up_int(LP * SR * (int)sizeof(T), 128) : 0;
+    }
+    __host__ __device__ int wrap_r_bytes(const StencilArgs& a) const {
+        return a.wrap_x && RP > 0 ? round_up_int(RP * SR * (int)sizeof(T), 128) : 0;
+    }
     // tile | coefficients (ncoef T) | compact list offsets (ncoef int) | compact list weights (ncoef T)
     __host__ __device__ size_t coef_off(const StencilArgs&) const { return round_up_int((int)tile_bytes(), 16); }
     __host__ __device__ size_t list_off(const StencilArgs& a) const {

@@ -73,20 +73,18 @@ cudaError_t launch_ldg(const StencilArgs& a, cudaStream_t s) {
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link-time libcuda dependency).
+// Looked up once (a function-local static: initialised once even when host threads race).
 inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-        else
-            cudaGetLastError();
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        cudaGetLastError();
+        return nullptr;
+    }();
     return fn;
 }
 
@@ -119,8 +117,11 @@ inline int sm_count() {
     return v;
 }
 
+// Resident threads per SM of the persistent FP32 grid (see launch_tma_mode).
+constexpr int kF32ThreadsPerSM = 768;
+
 // TMA path: returns cudaErrorNotSupported (without launching) when the geometry does not allow it.
-template <typename T, int TW, int TH, int RPT, int VEC, int S, int MODE>
+template <typename T, int TW, int TH, int RPT, int VEC, int S, int MODE, bool WRAP>
 cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
     TileGeom<T, TW, TH> g(a);
     // One box per window: at most 256 columns and 256 rows; rows and columns tile exactly; rows
@@ -129,16 +130,26 @@ cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
     TmaMaps maps;
     memset(&maps, 0, sizeof(maps));
     if (!encode_rows_map<T>(&maps.win, a.in, a.nx, a.rows, g.SW, g.SR)) return cudaErrorNotSupported;
+    // periodic in x: wrap-around boxes of the LP / RP edge columns (x = nx - LP and x = 0 are 16-byte
+    // aligned: rows are, and LP, RP are whole 16-byte units)
+    const int wl_bytes = WRAP ? g.wrap_l_bytes(a) : 0, wr_bytes = WRAP ? g.wrap_r_bytes(a) : 0;
+    if (wl_bytes && !encode_rows_map<T>(&maps.wrap_l, a.in, a.nx, a.rows, g.LP, g.SR)) return cudaErrorNotSupported;
+    if (wr_bytes && !encode_rows_map<T>(&maps.wrap_r, a.in, a.nx, a.rows, g.RP, g.SR)) return cudaErrorNotSupported;
     const size_t stage_bytes = round_up_int((int)((size_t)g.SR * g.SW * sizeof(T)), 128);
-    const size_t smem = S * stage_bytes + round_up_int(a.ncoef * (int)sizeof(T), 16) +
+    const size_t smem = S * (stage_bytes + wl_bytes + wr_bytes) + round_up_int(a.ncoef * (int)sizeof(T), 16) +
                         round_up_int(a.ncoef * (int)sizeof(int), 16) + round_up_int(a.ncoef * (int)sizeof(T), 16) +
                         256;   // 128 bytes of alignment slack for the ring base + tail padding
-    auto kern = stencil_tma_kernel<T, TW, TH, RPT, VEC, S, MODE>;
+    auto kern = stencil_tma_kernel<T, TW, TH, RPT, VEC, S, MODE, WRAP>;
     cudaError_t e = ensure_smem(kern, smem);
     if (e != cudaSuccess) return e == cudaErrorInvalidConfiguration ? cudaErrorNotSupported : e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (TW / VEC) * (TH / RPT), smem);
     if (e != cudaSuccess || per_sm < 1) return cudaErrorNotSupported;
+    // FP32 launches are bound by HBM, and more resident CTAs (each keeping S windows in flight) made
+    // them slower: over the twelve operators at 16384^2, 650 Gpts/s with every CTA that fits, 730
+    // capped at 768 threads per SM, 624 at 512. The FP64 launches, bound by the FP64 pipe, keep every
+    // CTA that fits (the 768 cap cost them 0.3%).
+    if (sizeof(T) == 4) per_sm = std::min(per_sm, std::max(1, kF32ThreadsPerSM / ((TW / VEC) * (TH / RPT))));
     const int tiles_x = a.nx / TW;
     const int tiles_total = tiles_x * (a.rows / TH);
     const int grid = std::min(tiles_total, per_sm * sm_count());
@@ -147,20 +158,32 @@ cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// The instantiation with or without the wrap-around boxes; the Y shapes have no columns to wrap.
+template <typename T, int TW, int TH, int RPT, int VEC, int S, int MODE>
+cudaError_t launch_tma_wrap(const StencilArgs& a, cudaStream_t s, bool wrap) {
+    if constexpr (MODE >= 5 && MODE <= 7) {
+        return launch_tma_mode<T, TW, TH, RPT, VEC, S, MODE, false>(a, s);
+    } else {
+        return wrap ? launch_tma_mode<T, TW, TH, RPT, VEC, S, MODE, true>(a, s)
+                    : launch_tma_mode<T, TW, TH, RPT, VEC, S, MODE, false>(a, s);
+    }
+}
+
 template <typename T, int TW, int TH, int RPT, int VEC, int S>
 cudaError_t launch_tma(const StencilArgs& a, cudaStream_t s) {
     const int mode = (variant_is_fun(a.variant) && !a.pre) ? (int)MODE_FUN : shape_mode(a.H, a.L, a.V, a.T);
+    const bool wrap = a.wrap_x && (a.L > 0 || a.R > 0);
     switch (mode) {
-    case MODE_FUN: return launch_tma_mode<T, TW, TH, RPT, VEC, S, MODE_FUN>(a, s);
-    case 2: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 2>(a, s);
-    case 3: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 3>(a, s);
-    case 4: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 4>(a, s);
-    case 5: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 5>(a, s);
-    case 6: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 6>(a, s);
-    case 7: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 7>(a, s);
-    case 8: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 8>(a, s);
-    case 9: return launch_tma_mode<T, TW, TH, RPT, VEC, S, 9>(a, s);
-    default: return launch_tma_mode<T, TW, TH, RPT, VEC, S, MODE_LIST>(a, s);
+    case MODE_FUN: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, MODE_FUN>(a, s, wrap);
+    case 2: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 2>(a, s, wrap);
+    case 3: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 3>(a, s, wrap);
+    case 4: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 4>(a, s, wrap);
+    case 5: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 5>(a, s, wrap);
+    case 6: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 6>(a, s, wrap);
+    case 7: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 7>(a, s, wrap);
+    case 8: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 8>(a, s, wrap);
+    case 9: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, 9>(a, s, wrap);
+    default: return launch_tma_wrap<T, TW, TH, RPT, VEC, S, MODE_LIST>(a, s, wrap);
     }
 }
 

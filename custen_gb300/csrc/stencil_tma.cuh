@@ -5,8 +5,11 @@
 // box of SW = LP + TW + RP columns by SR = T + TH + B rows starting at (x0 - LP, y0 - T), landing at a
 // 128-byte aligned stage. Completion is signalled on the stage's mbarrier (complete_tx); the next
 // tiles' copies run while the current tile computes. Rows and columns outside the launch arrive
-// zero-filled; edge tiles then fetch their halo rows through the halo pointers and their wrapped
-// columns (periodic variants) with plain loads -- two tile rows and two tile columns of the field.
+// zero-filled. Periodic variants add wrap-around boxes on the first and last tile column: the LP
+// columns left of x = 0 come from x = nx - LP, the RP columns right of nx from x = 0, each into a
+// side area of the stage on the same mbarrier, from where the edge tile copies them into place.
+// Edge tiles of the first and last tile row fetch their halo rows through the halo pointers with
+// plain (coalesced) loads.
 //
 // Every mbarrier wait is bounded: on expiry the CTA records an error in g_custen_device_error, waits
 // (bounded) for its own copies still in flight, and returns.
@@ -22,7 +25,9 @@ constexpr unsigned int kErrMbarrierTimeout = 1u;   // g_custen_device_error: che
 constexpr long long kWaitLimit = 1ll << 22;   // try_wait rounds (each may suspend ~µs) before giving up
 
 struct TmaMaps {
-    CUtensorMap win;   // launch rows, box {SW, SR}
+    CUtensorMap win;      // launch rows, box {SW, SR}
+    CUtensorMap wrap_l;   // periodic x: box {LP, SR}, read at x = nx - LP for the tiles at x0 = 0
+    CUtensorMap wrap_r;   // periodic x: box {RP, SR}, read at x = 0 for the tiles ending at nx
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -66,20 +71,32 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// Issue the copy of one tile window into the (128-byte aligned) stage `dst`.
+// Issue the copies of one tile window into the (128-byte aligned) stage `dst`: the window box, and on
+// the first / last tile column of a periodic launch the wrap-around boxes into the stage's side areas
+// `side` (LP x SR elements, then RP x SR from `side + wl_elems`).
 template <typename T, int TW, int TH>
-__device__ __forceinline__ void issue_window(const StencilArgs& a, const TmaMaps& m, T* dst, uint64_t* bar, int x0,
-                                             int y0, const TileGeom<T, TW, TH>& g) {
-    mbar_arrive_expect_tx(bar, (uint32_t)(g.SR * g.SW * sizeof(T)));
+__device__ __forceinline__ void issue_window(const StencilArgs& a, const TmaMaps& m, T* dst, T* side, int wl_elems,
+                                             int wr_elems, uint64_t* bar, int x0, int y0,
+                                             const TileGeom<T, TW, TH>& g) {
+    const bool left = wl_elems > 0 && x0 == 0;
+    const bool right = wr_elems > 0 && x0 + TW == a.nx;
+    uint32_t bytes = (uint32_t)(g.SR * g.SW * sizeof(T));
+    if (left) bytes += (uint32_t)(g.SR * g.LP * sizeof(T));
+    if (right) bytes += (uint32_t)(g.SR * g.RP * sizeof(T));
+    mbar_arrive_expect_tx(bar, bytes);
     tma_load_2d(dst, &m.win, x0 - g.LP, y0 - a.T, bar);
+    if (left) tma_load_2d(side, &m.wrap_l, a.nx - g.LP, y0 - a.T, bar);
+    if (right) tma_load_2d(side + wl_elems, &m.wrap_r, 0, y0 - a.T, bar);
 }
 
 // Edge tiles: replace the zero-filled cells outside the launch. Rows above / below the launch come
 // through the halo pointers (when the variant reads them); columns outside [0, nx) wrap around
-// (periodic variants). Cells with no source are left as zeros: no written point reads them.
+// (periodic variants): those of the rows inside the launch from the stage's side areas, filled by the
+// wrap-around boxes. Cells with no source are left as zeros: no written point reads them.
 template <typename T, int TW, int TH, int NT>
-__device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const TileGeom<T, TW, TH>& g, int x0, int y0,
-                                           int tid, bool rows_fix, bool cols_fix) {
+__device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const T* side, int wl_elems,
+                                           const TileGeom<T, TW, TH>& g, int x0, int y0, int tid, bool rows_fix,
+                                           bool cols_fix) {
     if (rows_fix) {
         // whole halo rows (all SW columns) of the rows outside [0, rows)
         const int total = g.SR * g.SW;
@@ -100,7 +117,11 @@ __device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const 
         }
     }
     if (cols_fix) {
-        // wrapped halo columns of the rows inside the launch
+        // wrapped halo columns of the rows inside the launch, from the side areas: column k < LP of
+        // row r is side[r * LP + k] (x = nx - LP + k), column LP + TW + k is side_r[r * RP + k] (x = k);
+        // the boxes zero-fill x outside [0, nx) as a too-narrow field needs
+        const bool left = x0 == 0, right = x0 + TW == a.nx;
+        const T* side_r = side + wl_elems;
         const int ncols = g.LP + g.RP;
         const int total = g.SR * ncols;
         for (int e = tid; e < total; e += NT) {
@@ -108,13 +129,16 @@ __device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const 
             const int gyl = y0 - a.T + r;
             if (gyl < 0 || gyl >= a.rows) continue;
             const int k = e - r * ncols;
-            const int c = (k < g.LP) ? k : (g.LP + TW + (k - g.LP));
-            const int x = x0 - g.LP + c;
-            if (x >= 0 && x < a.nx) continue;
-            const int xw = x < 0 ? x + a.nx : x - a.nx;
-            if (xw < 0 || xw >= a.nx) continue;
-            if (!in_bounds((long long)r * g.SW + c, 0, (long long)g.SR * g.SW)) continue;
-            tile[r * g.SW + c] = __ldg(reinterpret_cast<const T*>(a.in) + (size_t)gyl * a.nx + xw);
+            if (k < g.LP) {
+                if (!left) continue;
+                if (!in_bounds((long long)r * g.SW + k, 0, (long long)g.SR * g.SW)) continue;
+                tile[r * g.SW + k] = side[r * g.LP + k];
+            } else {
+                if (!right) continue;
+                const int kk = k - g.LP;
+                if (!in_bounds((long long)r * g.SW + g.LP + TW + kk, 0, (long long)g.SR * g.SW)) continue;
+                tile[r * g.SW + g.LP + TW + kk] = side_r[r * g.RP + kk];
+            }
         }
     }
 }
@@ -126,7 +150,9 @@ __device__ __forceinline__ void edge_fixup(const StencilArgs& a, T* tile, const 
 // mode, whose indirect calls need more registers).
 constexpr int min_blocks_for(int threads, bool fun) { return (fun ? 512 : 768) / threads > 0 ? (fun ? 512 : 768) / threads : 1; }
 
-template <typename T, int TW, int TH, int RPT, int VEC, int S, int MODE>
+// WRAP: the launch is periodic in x with a left or right halo (wrap-around boxes and side areas); the
+// other launches run an instantiation without them, which keeps their register allocation.
+template <typename T, int TW, int TH, int RPT, int VEC, int S, int MODE, bool WRAP>
 __global__ void __launch_bounds__((TW / VEC) * (TH / RPT), min_blocks_for((TW / VEC) * (TH / RPT), MODE == MODE_FUN))
 stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__ StencilArgs a, int tiles_x,
                    int tiles_total) {
@@ -145,7 +171,11 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
     asm volatile("" : "+r"(raw_addr));
     unsigned char* smem = smem_raw + ((128u - (raw_addr & 127u)) & 127u);
     T* ring = reinterpret_cast<T*>(smem);
-    unsigned char* after = smem + S * stage_bytes;
+    // side areas of the wrap-around boxes, per stage (zero-sized unless the launch wraps in x)
+    const int wl_bytes = WRAP ? g.wrap_l_bytes(a) : 0, wr_bytes = WRAP ? g.wrap_r_bytes(a) : 0;
+    const int wl_elems = wl_bytes / (int)sizeof(T), wr_elems = wr_bytes / (int)sizeof(T);
+    T* sides = reinterpret_cast<T*>(smem + S * stage_bytes);
+    unsigned char* after = smem + S * (stage_bytes + wl_bytes + wr_bytes);
     T* coef_s = reinterpret_cast<T*>(after);
     int* list_off = reinterpret_cast<int*>(after + round_up_int(a.ncoef * (int)sizeof(T), 16));
     T* list_w = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(list_off) +
@@ -160,8 +190,9 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
             const int t = blockIdx.x + k * gridDim.x;
             if (t >= tiles_total) break;
             const int tyi = t / tiles_x, txi = t - tyi * tiles_x;
-            issue_window<T, TW, TH>(a, maps, ring + (size_t)k * stage_bytes / sizeof(T), &full[k], txi * TW,
-                                    tyi * TH, g);
+            issue_window<T, TW, TH>(a, maps, ring + (size_t)k * stage_bytes / sizeof(T),
+                                    sides + (size_t)k * (wl_elems + wr_elems), wl_elems, wr_elems, &full[k],
+                                    txi * TW, tyi * TH, g);
         }
     }
     const int nlist = stage_coefficients<T, NT>(a, coef_s, list_off, list_w, g.SW, tid, is_fun);  // syncs
@@ -172,6 +203,7 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
         const int s = it % S;
         const uint32_t parity = (uint32_t)((it / S) & 1);
         T* tile = ring + (size_t)s * stage_bytes / sizeof(T);
+        T* side = sides + (size_t)s * (wl_elems + wr_elems);
         // Each thread waits on the stage itself (the wait acquires the copy's data for that thread), so
         // no barrier is needed before reading it. A thread whose wait expired skips the tile's compute;
         // the end-of-tile barrier then makes the exit decision uniform.
@@ -179,9 +211,9 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
         const int tyi = t / tiles_x, txi = t - tyi * tiles_x;
         const int x0 = txi * TW, y0 = tyi * TH;
         const bool rows_fix = (y0 == 0 && a.T > 0 && a.has_top) || (y0 + TH == a.rows && a.B > 0 && a.has_bot);
-        const bool cols_fix = a.wrap_x && (x0 == 0 || x0 + TW == a.nx) && (a.L > 0 || a.R > 0);
+        const bool cols_fix = WRAP && (x0 == 0 || x0 + TW == a.nx);
         if (rows_fix || cols_fix) {
-            edge_fixup<T, TW, TH, NT>(a, tile, g, x0, y0, tid, rows_fix, cols_fix);
+            edge_fixup<T, TW, TH, NT>(a, tile, side, wl_elems, g, x0, y0, tid, rows_fix, cols_fix);
             __syncthreads();
         }
         if (a.pre) {
@@ -222,7 +254,7 @@ stencil_tma_kernel(const __grid_constant__ TmaMaps maps, const __grid_constant__
             const int tn = t + S * gridDim.x;
             if (tn < tiles_total) {
                 const int tyn = tn / tiles_x, txn = tn - tyn * tiles_x;
-                issue_window<T, TW, TH>(a, maps, tile, &full[s], txn * TW, tyn * TH, g);
+                issue_window<T, TW, TH>(a, maps, tile, side, wl_elems, wr_elems, &full[s], txn * TW, tyn * TH, g);
             }
         }
     }
