@@ -319,6 +319,35 @@ def test_tma_path_periodic_edges_wide_halo(gpu, variant):
     check(got, ref, st, pre)
 
 
+def _wrap_box_cases():
+    """(variant, (H, L, R, V, T, B), fun_id): halos on the left only, on the right only, and uneven."""
+    cases = []
+    for L, R in ((3, 0), (0, 2), (1, 4)):
+        cases.append((cs.XP, (L + R + 1, L, R, 1, 0, 0), -1))
+        cases.append((cs.XYP, (L + R + 1, L, R, 4, 2, 1), -1))
+        cases.append((cs.XYPFUN, (L + R + 1, L, R, 4, 2, 1), FUN_IDS[2][1]))
+    cases.append((cs.XPFUN, (5, 2, 2, 1, 0, 0), FUN_IDS[0][1]))   # the 5-point x function
+    return cases
+
+
+@pytest.mark.parametrize("case", _wrap_box_cases(),
+                         ids=lambda c: f"{cs.VARIANT_NAMES[c[0]]}-L{c[1][1]}R{c[1][2]}")
+@pytest.mark.parametrize("tiles_x", [1, 2])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["f64", "f32"])
+def test_tma_wrap_boxes(gpu, case, tiles_x, dtype):
+    """Wrap-around boxes of the periodic edge columns in the TMA kernel (configuration 0: 64-column FP64
+    and 128-column FP32 tiles). With one tile column both boxes land on the same tile; with a halo on one
+    side only, one box is issued. Bit-exact, and the TMA kernel is the one that ran."""
+    variant, geom, fun_id = case
+    nx = (64 if dtype == np.float64 else 128) * tiles_x
+    before = cs.kernel_launches_tma()
+    got, ref, st, pre = run_both(variant, nx, 64, 1, 16, 8, geom, dtype=dtype, fun_id=fun_id,
+                                 seed=nx + geom[1] * 10 + geom[2], config=0)
+    assert cs.kernel_launches_tma() > before, "the TMA-staged kernel did not run"
+    check(got, ref, st, pre)
+    assert cs.device_error() == 0
+
+
 SHAPES = {  # the compile-time register-window shapes: (variant, H, L, R, V, T, B)
     "X3": (cs.XP, 3, 1, 1, 1, 0, 0), "X5": (cs.XNP, 5, 2, 2, 1, 0, 0), "X9": (cs.XP, 9, 4, 4, 1, 0, 0),
     "Y3": (cs.YNP, 1, 0, 0, 3, 1, 1), "Y5": (cs.YP, 1, 0, 0, 5, 2, 2), "Y9": (cs.YP, 1, 0, 0, 9, 4, 4),
