@@ -382,6 +382,33 @@ static cudaError_t copy_tile_rows(const cuSten_t* h, int t, int r_begin, int r_e
     return cudaSuccess;
 }
 
+// Untouched output columns of a non-periodic chunk: the first lw and the last rw 4-byte words of each of
+// `rows` rows, read in place from device-accessible (pinned or registered) host memory into the output
+// slot. One small gather per chunk instead of two strided copies of a few bytes per row, which the copy
+// engines move one row at a time.
+__global__ void stage_edge_columns_kernel(uint32_t* slot, const uint32_t* host, size_t row_words, int rows, int lw,
+                                          int rw) {
+    const int per_row = lw + rw;
+    const long long total = (long long)rows * per_row;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long r = e / per_row;
+        const int k = (int)(e - r * per_row);
+        const size_t col = k < lw ? (size_t)k : row_words - (size_t)rw + (size_t)(k - lw);
+        slot[(size_t)r * row_words + col] = host[(size_t)r * row_words + col];
+    }
+}
+
+// Device address of host memory the GPU can read in place (pinned or registered), else null.
+static const char* mapped_host(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? static_cast<const char*>(at.devicePointer) : nullptr;
+}
+
 // Host-resident fields: the rows of every tile stream through device staging slots in chunks.
 // Chunk c copies its input rows and halo rows in on s_in, computes on s_comp and copies its output
 // rows back on s_out; kStageSlots chunks are in flight, so the two copy directions and the
@@ -436,6 +463,8 @@ static int compute_staged(cuSten_t* h, PlanPrivate* p, StencilArgs& a, cudaStrea
     const int wl = std::max(p->L, p->R);
     int c = 0;
     for (int t = 0; t < nt; ++t) {
+        // untouched output columns are gathered by a kernel where the output tile is mapped host memory
+        const char* out_mapped = (!periodic && dir != 1) ? mapped_host(h->dataOutput[t]) : nullptr;
         for (int r0 = 0; r0 < nyT; r0 += rows, ++c) {
             const int rc = std::min(rows, nyT - r0);
             const int k = c % kStageSlots;
@@ -468,7 +497,17 @@ static int compute_staged(cuSten_t* h, PlanPrivate* p, StencilArgs& a, cudaStrea
                         h2d += bytes;
                     }
                 }
-                if (dir != 1) {
+                const int lw_words = p->L * esz / 4, rw_words = wl * esz / 4;
+                if (dir != 1 && out_mapped != nullptr && lw_words + rw_words > 0) {
+                    const long long words = (long long)rc * (lw_words + rw_words);
+                    const int blocks = (int)std::min<long long>((words + 255) / 256, 1024);
+                    stage_edge_columns_kernel<<<blocks, 256, 0, s_in>>>(
+                        reinterpret_cast<uint32_t*>(out_slot),
+                        reinterpret_cast<const uint32_t*>(out_mapped + (size_t)r0 * row_bytes), row_bytes / 4, rc,
+                        lw_words, rw_words);
+                    CU_TRY(cudaGetLastError(), "Copying untouched output columns");
+                    h2d += (size_t)(lw_words + rw_words) * 4 * rc;
+                } else if (dir != 1) {
                     if (p->L > 0) {
                         CU_TRY(cudaMemcpy2DAsync(out_slot, row_bytes, host_out, row_bytes, (size_t)p->L * esz, rc,
                                                  cudaMemcpyDefault, s_in),
