@@ -382,6 +382,17 @@ def run_gpu(args, world, rank, local):
     ops = operators(n)
     stream = torch.cuda.current_stream(dev)
 
+    # ---- e2e: reference-facing API with host buffers (numTiles=4, HOST offload) ----
+    # The e2e legs run first. On this machine sustained GPU compute slows host<->device DMA for a while
+    # afterwards (in bursts, for minutes); an e2e workload by itself does not, so the e2e is measured
+    # before this process's compute legs rather than after them. e2e.link carries the host link
+    # measured alongside it.
+    e2e = e2e_managed = None
+    if not args.skip_e2e:
+        e2e = run_e2e(args, cs, np, local, ops, "pinned")
+        if not args.skip_e2e_managed:
+            e2e_managed = run_e2e(args, cs, np, local, ops, "managed", steps=1)
+
     def make_field(dtype):
         x = torch.arange(n, device=dev, dtype=torch.float64) * (2 * math.pi / n)
         g = torch.Generator(device=dev)
@@ -461,16 +472,6 @@ def run_gpu(args, world, rank, local):
                    "config": hs64[len(per)].config(),
                    "hbm_gbs": round(16.0 * n * n / (ms * 1e-3) / 1e9, 1),
                    "fp64_frac": round(dfma_pt * n * n / (ms * 1e-3) / fp64_rate, 3)}
-
-    # ---- e2e: reference-facing API with host buffers (numTiles=4, HOST offload) ----
-    # The e2e legs run early, before the legs that build multi-GiB host arrays. The staged e2e reaches
-    # 0.5-0.9 of the host link measured alongside it, from one process to the next, with every host
-    # buffer copying at full rate on its own (e2e.link carries both measurements).
-    e2e = e2e_managed = None
-    if not args.skip_e2e:
-        e2e = run_e2e(args, cs, np, local, ops, "pinned")
-        if not args.skip_e2e_managed:
-            e2e_managed = run_e2e(args, cs, np, local, ops, "managed", steps=1)
 
     # ---- the six Fun operators again with the indirect call (library function fusion off) ----
     fun_indirect = None
