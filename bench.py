@@ -191,6 +191,17 @@ def cpu_sample(n: int, rows: int, threads: int):
     return one_pass
 
 
+def cpu_single_thread(n: int, rows: int = 256) -> dict:
+    """The same plain host loop on one thread, over a smaller sample of rows."""
+    one = cpu_sample(n, rows, 1)
+    one()
+    t0 = time.perf_counter()
+    pts = one()
+    dt = time.perf_counter() - t0
+    return {"value": round(pts / dt / 1e9, 4), "unit": "Gpts/s", "cores": 1,
+            "sample": f"{rows} rows x {n} columns per operator, 12 operators, plain host loop, 1 thread"}
+
+
 def cpu_ch_sample(steps: int = 40, n: int = 256) -> dict:
     """The serial Cahn-Hilliard solver (oracle port of cuPentSpeedUp/serialCahnADITiming/serialCahnADI.c,
     single-threaded as the reference program is) on config 1's grid: 256^2, lx = 2 pi, bounded steps."""
@@ -346,7 +357,8 @@ def run_reference_arm(args, world, rank):
         "config": {"workload": f"stencil sweep FP64 {args.n}^2, 12 cuSten operators (sample of {rows} rows each)",
                    "nx": args.n, "ny": args.n},
         "cpu_baseline": {"value": round(v, 4), "unit": "Gpts/s", "cores": threads, "kind": "port",
-                         "sample": f"{rows} rows x {args.n} columns per operator, 12 operators, plain host loop"},
+                         "sample": f"{rows} rows x {args.n} columns per operator, 12 operators, plain host loop",
+                         "single_thread": cpu_single_thread(args.n)},
         "e2e": {"value": round(v, 4), "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "cpu_ch": cpu_ch_sample(),
     }
@@ -537,7 +549,8 @@ def run_gpu(args, world, rank, local):
         dtc = time.perf_counter() - t0c
         cpu = {"value": round(pts / dtc / 1e9, 4), "unit": "Gpts/s", "cores": threads, "kind": "port",
                "sample": f"{args.cpu_rows} rows x {n} columns per operator, 12 operators, plain host loop, "
-                         f"{threads} threads"}
+                         f"{threads} threads",
+               "single_thread": cpu_single_thread(n)}
 
     for h in hs64:
         h.destroy()
