@@ -210,7 +210,7 @@ def test_host_memory_streaming(gpu, small_chunks, variant, tiles, mem):
     assert h2d1 - h2d0 >= nx * ny * 8            # every input row goes in at least once
 
 
-@pytest.mark.parametrize("variant", [cs.XP, cs.YNP, cs.XYP, cs.XYNP])
+@pytest.mark.parametrize("variant", [cs.XP, cs.XNP, cs.YNP, cs.XYP, cs.XYNP])
 def test_host_memory_default_chunks_f32(gpu, variant):
     """Pinned FP32 fields at the default chunk size, DEVICE offload (the output still lands in host
     memory: it is where the field lives)."""
