@@ -36,33 +36,10 @@ sys.path.insert(0, str(ROOT))
 # (profiles/stencil_sweep_traffic.md); the field is streamed once per launch, so it scales with n^2.
 TRAFFIC_6144 = 559918997.0
 
-W5 = [-1.0, 16.0, -30.0, 16.0, -1.0]
-WCROSS = [1.0, 0.0, -1.0, 0.0, 0.0, 0.0, -1.0, 0.0, 1.0]
-WLAP = [0.0, 1.0, 0.0, 1.0, -4.0, 1.0, 0.0, 1.0, 0.0]
-
-
 def operators(n: int):
-    """(name, variant, H, L, R, V, T, B, weights, fun_id, dfma_per_point)"""
-    h = 2 * math.pi / n
-    w5 = [w / (12 * h * h) for w in W5]
-    wc = [w / (4 * h * h) for w in WCROSS]
-    wl = [w / (h * h) for w in WLAP]
-    # FP64 operations per point: weights skip exact zeros; the Fun variants run the library's c^3 - c
-    # functions fused: c^3 - c (mul + fma) once per input value, then an fma per non-zero coefficient.
-    ops = []
-    for nm, v in (("Xp", 0), ("Xnp", 1)):
-        ops.append((nm, v, 5, 2, 2, 1, 0, 0, w5, -1, 5))
-    for nm, v in (("XpFun", 2), ("XnpFun", 3)):
-        ops.append((nm, v, 5, 2, 2, 1, 0, 0, w5, 1, 7))
-    for nm, v in (("Yp", 4), ("Ynp", 5)):
-        ops.append((nm, v, 1, 0, 0, 5, 2, 2, w5, -1, 5))
-    for nm, v in (("YpFun", 6), ("YnpFun", 7)):
-        ops.append((nm, v, 1, 0, 0, 5, 2, 2, w5, 3, 7))
-    for nm, v in (("XYp", 8), ("XYnp", 9)):
-        ops.append((nm, v, 3, 1, 1, 3, 1, 1, wc, -1, 4))
-    for nm, v in (("XYpFun", 10), ("XYnpFun", 11)):
-        ops.append((nm, v, 3, 1, 1, 3, 1, 1, wl, 5, 7))
-    return ops
+    """(name, variant, H, L, R, V, T, B, weights, fun_id, dfma_per_point) of the 12-operator sweep."""
+    from custen_gb300.inputs import sweep_operators
+    return sweep_operators(n)
 
 
 def dist_setup():
@@ -165,7 +142,7 @@ def cpu_sample(n: int, rows: int, threads: int):
     import numpy as np
 
     import oracle
-    from tests.helpers import field
+    from custen_gb300.inputs import field
     oracle.build()
     # rows sampled from the real n x n field: build only the rows the sample reads (+ halos)
     full_rows = rows + 4
@@ -688,7 +665,7 @@ def run_e2e(args, cs, np, local, ops, kind="pinned", steps=None):
     def arr(ptr, count):
         return np.frombuffer((ctypes.c_char * (8 * count)).from_address(ptr), dtype=np.float64)
 
-    from tests.helpers import field
+    from custen_gb300.inputs import field
     inp = host(nbytes)
     arr(inp, n * n)[:] = field(n, n, 1).ravel()
     outs, hs = [], []

@@ -68,6 +68,8 @@ def lib() -> ctypes.CDLL:
         L.custen_set_config.argtypes = [vp, i]
         L.custen_set_fun_fusion.argtypes = [i]
         L.custen_set_fun_fusion.restype = None
+        L.custen_set_max_ctas.argtypes = [i]
+        L.custen_set_max_ctas.restype = None
         L.custen_builtin_fun_id.argtypes = [vp, i]
         L.custen_device_error.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
         L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
@@ -206,6 +208,11 @@ def tune_cache_path() -> str:
 def set_fun_fusion(enable: bool) -> None:
     """Fused path for the library's own c^3 - c Fun functions (default on); off = indirect calls."""
     lib().custen_set_fun_fusion(int(bool(enable)))
+
+
+def set_max_ctas(max_ctas: int) -> None:
+    """Cap the CTAs of a persistent stencil launch (0: no cap). Results do not depend on it."""
+    lib().custen_set_max_ctas(int(max_ctas))
 
 
 def set_stage_chunk_bytes(nbytes: int) -> None:

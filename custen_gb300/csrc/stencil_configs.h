@@ -44,6 +44,10 @@ constexpr StencilConfig kConfigsF32[kNumConfigs] = {
 // the TMA-staged kernel ran, 0 for the plain-load kernel.
 cudaError_t launch_stencil_cfg(const StencilArgs& a, int dtype, int cfg, cudaStream_t s, int* path);
 
+// Upper bound on the CTAs of a persistent stencil launch (0: none, the default). Lowering it makes each
+// CTA walk more tiles through its shared-memory ring, so that small fields exercise stage reuse.
+int persistent_grid_cap();
+
 // "f64_tw64_th32_rpt4_vec2" and the like.
 const char* config_name(int dtype, int cfg);
 

@@ -1,4 +1,5 @@
 // Routes a stencil launch to the kernel configuration a handle uses (stencil_configs.h).
+#include <atomic>
 #include <cstdio>
 
 #include "stencil_configs.h"
@@ -22,6 +23,10 @@ static const LaunchFn kLaunchF32[] = {launch_cfg_1_0, launch_cfg_1_1, launch_cfg
                                       launch_cfg_1_3, launch_cfg_1_4, launch_cfg_1_5};
 static_assert(sizeof(kLaunchF64) / sizeof(LaunchFn) == kNumConfigs, "one FP64 launcher per configuration");
 static_assert(sizeof(kLaunchF32) / sizeof(LaunchFn) == kNumConfigs, "one FP32 launcher per configuration");
+
+static std::atomic<int> g_grid_cap{0};
+
+int persistent_grid_cap() { return g_grid_cap.load(std::memory_order_relaxed); }
 
 cudaError_t launch_stencil_cfg(const StencilArgs& a, int dtype, int cfg, cudaStream_t s, int* path) {
     if (cfg < 0 || cfg >= kNumConfigs) cfg = 0;
@@ -57,3 +62,5 @@ const char* config_name(int dtype, int cfg) {
 }
 
 }  // namespace custen
+
+extern "C" void custen_set_max_ctas(int max_ctas) { custen::g_grid_cap.store(max_ctas > 0 ? max_ctas : 0); }

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cstring>
 
+#include "stencil_configs.h"
 #include "stencil_kernel.cuh"
 #include "stencil_tma.cuh"
 
@@ -152,7 +153,9 @@ cudaError_t launch_tma_mode(const StencilArgs& a, cudaStream_t s) {
     if (sizeof(T) == 4) per_sm = std::min(per_sm, std::max(1, kF32ThreadsPerSM / ((TW / VEC) * (TH / RPT))));
     const int tiles_x = a.nx / TW;
     const int tiles_total = tiles_x * (a.rows / TH);
-    const int grid = std::min(tiles_total, per_sm * sm_count());
+    int grid = std::min(tiles_total, per_sm * sm_count());
+    const int cap = persistent_grid_cap();
+    if (cap > 0) grid = std::min(grid, cap);
     dim3 block(TW / VEC, TH / RPT);
     kern<<<grid, block, smem, s>>>(maps, a, tiles_x, tiles_total);
     return cudaGetLastError();

@@ -49,6 +49,10 @@ void custen_set_stage_chunk_bytes(size_t bytes);
  * coefficients as plain weights: bit-identical results, fewer FP64 operations. enable = 0 sends them
  * through the indirect call like any user function. Default 1. No reference counterpart. */
 void custen_set_fun_fusion(int enable);
+/* At most `max_ctas` CTAs per persistent (TMA-staged) stencil launch; 0 (the default) lifts the cap.
+ * Results do not depend on it: a lower cap makes each CTA walk more tiles through its shared-memory
+ * ring, which lets small fields exercise stage reuse. No reference counterpart. */
+void custen_set_max_ctas(int max_ctas);
 /* ---- autotuner (no reference counterpart) ----
  * The stencil kernels come in several tile configurations (tile width / height, rows per thread, vector
  * width: the role of BLOCK_X / BLOCK_Y); all compute identical values. A handle's first Compute on

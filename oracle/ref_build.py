@@ -1,7 +1,8 @@
 """Builds the reference's own code from the reference sources into oracle/_ref -- TEST INFRASTRUCTURE ONLY.
 
 Nothing is copied out of the reference: the wrappers below #include the reference files where they
-lie (REF_ROOT, by default the read-only reference checkout), and only build outputs land in
+lie (the reference root: $CUSTEN_REFERENCE_ROOT, else a checkout named `reference` beside this
+repository, else nothing is built), and only build outputs land in
 oracle/_ref (git-ignored). Where the sources are absent (e.g. on the GPU machine) nothing is built
 and the prebuilt outputs are used if they are present.
 
@@ -26,7 +27,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
-REF = Path(os.environ.get("CUSTEN_REFERENCE_ROOT", "/root/reference"))
+REF = Path(os.environ["CUSTEN_REFERENCE_ROOT"]) if os.environ.get("CUSTEN_REFERENCE_ROOT") else ROOT.parent / "reference"
 OUT = HERE / "_ref"
 CUBIN = OUT / "custen_ref_sm103a.cubin"
 CH_CUBIN = OUT / "custen_ref_ch_sm103a.cubin"
@@ -91,5 +92,8 @@ def build_if_available() -> None:
 
 
 if __name__ == "__main__":
+    import sys
+    if len(sys.argv) > 1:   # python oracle/ref_build.py <reference root>
+        REF = Path(sys.argv[1])
     build_if_available()
     print(sorted(p.name for p in OUT.glob("*")) if OUT.exists() else "reference sources not present")

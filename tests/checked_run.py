@@ -15,7 +15,8 @@ assert os.environ.get("CUSTEN_CHECKED") == "1", "run with CUSTEN_CHECKED=1"
 
 import custen_gb300 as cs  # noqa: E402
 import oracle  # noqa: E402
-from tests.helpers import DeviceBuffer, weno_inputs  # noqa: E402
+from custen_gb300.buffers import DeviceBuffer  # noqa: E402
+from custen_gb300.inputs import weno_inputs
 from tests.test_stencil_parity import FUN_IDS, check, geometry, run_both  # noqa: E402
 
 

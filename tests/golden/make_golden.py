@@ -3,7 +3,7 @@
 
 Run on a GPU machine that has oracle/_ref/custen_ref_sm103a.cubin:
     python tests/golden/make_golden.py [output.npz]
-Inputs are regenerated from their seeds (tests/helpers.py: field, weights_for); only the reference
+Inputs are regenerated from their seeds (custen_gb300/inputs.py: field; tests/helpers.py: weights_for); only the reference
 outputs, the configurations and the pre-fill are stored. tests/test_golden.py checks the CPU oracle
 against these fixtures.
 """
@@ -17,7 +17,9 @@ sys.path.insert(0, str(ROOT))
 
 import custen_gb300 as cs  # noqa: E402
 import oracle  # noqa: E402
-from tests.helpers import DeviceBuffer, field, sentinel, weights_for  # noqa: E402
+from custen_gb300.buffers import DeviceBuffer  # noqa: E402
+from custen_gb300.inputs import field, sentinel  # noqa: E402
+from tests.helpers import weights_for  # noqa: E402
 
 # (variant, nx, ny, tiles, bx, by, H, L, R, V, T, B, fun_id)
 CONFIGS = []

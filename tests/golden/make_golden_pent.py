@@ -4,7 +4,7 @@ oracle/ref_build.py) on the GPU.
 
 Run on a GPU machine that has oracle/_ref/custen_ref_ch_sm103a.cubin:
     python tests/golden/make_golden_pent.py [output.npz]
-Inputs are regenerated from their seeds (tests/helpers.py: pent_system); the factors and solutions the
+Inputs are regenerated from their seeds (custen_gb300/inputs.py: pent_system); the factors and solutions the
 reference kernels produce are stored. tests/test_pent_oracle.py checks the CPU oracle against them.
 """
 import sys
@@ -16,7 +16,8 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
 import oracle  # noqa: E402
-from tests.helpers import DeviceBuffer, pent_system  # noqa: E402
+from custen_gb300.buffers import DeviceBuffer  # noqa: E402
+from custen_gb300.inputs import pent_system  # noqa: E402
 
 CONFIGS = [(4, 33), (5, 64), (32, 96), (61, 50)]   # (m, batch)
 

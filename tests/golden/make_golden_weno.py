@@ -15,7 +15,8 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
 import oracle  # noqa: E402
-from tests.helpers import DeviceBuffer, weno_inputs  # noqa: E402
+from custen_gb300.buffers import DeviceBuffer  # noqa: E402
+from custen_gb300.inputs import weno_inputs  # noqa: E402
 
 # (nx, ny, numTiles, BLOCK_X, BLOCK_Y, rough): at least two blocks per direction and per tile, as the
 # reference kernel assumes

@@ -35,7 +35,9 @@ def test_configurations_on_unaligned_geometry(gpu, config):
 
 
 def test_autotune_caches_and_reuses(gpu, tmp_path):
-    from tests.helpers import DeviceBuffer, field, weights_for
+    from custen_gb300.buffers import DeviceBuffer
+    from custen_gb300.inputs import field
+    from tests.helpers import weights_for
     cache = tmp_path / "tune.json"
     cs.set_tune_cache(str(cache))
     assert cs.tune_cache_path() == str(cache)

@@ -39,6 +39,25 @@ def test_served_results_equal_alone(gpu):
     srv.close()
 
 
+def test_served_2048_request_in_mix_equals_alone(gpu):
+    """A 2048^2 request served in a mix of smaller ones that arrive while it runs: bit-identical to its run
+    alone, mass conserved; the smaller requests likewise."""
+    reqs = [(2048, 12, 0.0), (512, 20, 0.0), (128, 30, 0.01), (1024, 8, 0.02), (256, 16, 0.05)]
+    rng = np.random.default_rng(78)
+    c0s = [rng.uniform(-0.1, 0.1, (n, n)) for n, _, _ in reqs]
+    srv = cs.CahnHilliardServer(hbm_budget_bytes=4e9, chunk_steps=4)
+    ids = [srv.submit(n, s, arrival=a, c0=c) for (n, s, a), c in zip(reqs, c0s)]
+    srv.run()
+    st = srv.stats()
+    assert st["steps"] == sum(s for _, s, _ in reqs)
+    assert st["max_active"] >= 2, "requests should overlap on the device"
+    for rid, (n, s, a), c in zip(ids, reqs, c0s):
+        r = srv.result(rid)
+        assert np.array_equal(r["field"], _alone(n, c, s)), f"request {rid} ({n}^2) differs from its run alone"
+        assert abs(r["mean_end"] - r["mean0"]) <= 1e-12
+    srv.close()
+
+
 def test_budget_limits_resident_set(gpu):
     """A budget that holds two 128^2 grids at a time: four requests still all complete."""
     per_grid = 3 * 128 * 128 * 8 + 2 * 128 * 8

@@ -93,9 +93,49 @@ def test_graph_and_plain_launches_agree(gpu):
     assert np.array_equal(outs[0], outs[1])
 
 
-def test_fp32_stencil_variant_error_reported(gpu):
-    """FP32 explicit terms, FP64 solve: the error against the FP64 oracle is bounded and mass holds."""
-    n, steps = 128, 50
+def test_large_grids_uneven_batch_match_oracle(gpu):
+    """Grids of 512^2, 1024^2 and 2048^2 (the sizes the batched and served workloads run) in one uneven batch
+    with two small grids, 20 steps: each grid within rel L2 1e-10 of the oracle with its mean conserved to
+    1e-12, and bit-identical to the same grid advanced alone. At these sizes the x sweep walks 16-64 chunks of
+    32 columns per line and the persistent work lists hold many more items than CTAs."""
+    sizes = [2048, 96, 512, 1024, 64]
+    steps = 20
+    c0s = [c0_for(n, 60 + k) for k, n in enumerate(sizes)]
+    b = cs.CahnHilliardBatch(sizes)
+    for k, c in enumerate(c0s):
+        b.set_state(k, c)
+    b.step(steps)
+    b.synchronize()
+    for k, n in enumerate(sizes):
+        mix, mix_old = b.state(k)
+        ref = oracle.CHOracle(c0s[k])
+        ref.step(steps)
+        rcur, rold = ref.fields()
+        err = rel_l2(mix, rcur)
+        drift = abs(b.mean(k) - oracle.compensated_mean(c0s[k]))
+        print(f"{n}^2 x {steps} steps in the batch: rel L2 {err:.3e}, mass drift {drift:.3e}")
+        assert err <= REL_L2, n
+        assert rel_l2(mix_old, rold) <= REL_L2, n
+        assert drift <= MASS, n
+        if n >= 512:
+            alone = cs.CahnHilliardBatch([n])
+            alone.set_state(0, c0s[k])
+            alone.step(steps)
+            a, a_old = alone.state(0)
+            alone.close()
+            assert np.array_equal(mix, a) and np.array_equal(mix_old, a_old), f"{n}^2 differs alone vs in the batch"
+    b.close()
+
+
+# FP32 explicit terms, FP64 solve and FP64 compensated mass sum: relative L2 against the FP64 oracle grows
+# with the step count; the mass is summed in FP64.
+FP32_REL_L2 = 1e-5
+
+
+@pytest.mark.parametrize("n,steps", [(128, 50), (512, 50)])
+def test_fp32_stencil_variant_error_reported(gpu, n, steps):
+    """FP32 explicit terms, FP64 solve: the error against the FP64 oracle stays under the stated bound and
+    mass holds to the FP64 bar."""
     c0 = c0_for(n, 5)
     b = cs.CahnHilliardBatch([n], rhs_dtype=cs.F32)
     b.set_state(0, c0)
@@ -105,9 +145,9 @@ def test_fp32_stencil_variant_error_reported(gpu):
     ref.step(steps)
     err = rel_l2(cur, ref.fields()[0])
     drift = abs(b.mean(0) - oracle.compensated_mean(c0))
-    print(f"FP32-stencil variant 128^2 x 50: rel L2 {err:.3e}, mass drift {drift:.3e}")
-    assert err < 1e-3
-    assert drift < 1e-6
+    print(f"FP32-stencil variant {n}^2 x {steps}: rel L2 {err:.3e}, mass drift {drift:.3e}")
+    assert err < FP32_REL_L2
+    assert drift <= MASS
     b.close()
 
 

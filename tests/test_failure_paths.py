@@ -14,7 +14,8 @@ import pytest
 
 import custen_gb300 as cs
 import oracle
-from tests.helpers import DeviceBuffer, field, sentinel
+from custen_gb300.buffers import DeviceBuffer
+from custen_gb300.inputs import field, sentinel
 
 pytestmark = pytest.mark.gpu
 

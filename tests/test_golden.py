@@ -6,7 +6,8 @@ import numpy as np
 import pytest
 
 import oracle
-from tests.helpers import field, sentinel, weights_for
+from custen_gb300.inputs import field, sentinel
+from tests.helpers import weights_for
 
 GOLDEN = Path(__file__).with_name("golden") / "reference_kernels.npz"
 

@@ -6,7 +6,9 @@ import pytest
 
 import custen_gb300 as cs
 import oracle
-from tests.helpers import DeviceBuffer, pent_dense_apply, pent_system
+from custen_gb300.buffers import DeviceBuffer
+from custen_gb300.inputs import pent_system
+from tests.helpers import pent_dense_apply
 
 pytestmark = pytest.mark.gpu
 

@@ -6,7 +6,8 @@ import numpy as np
 import pytest
 
 import oracle
-from tests.helpers import pent_dense_apply, pent_system
+from custen_gb300.inputs import pent_system
+from tests.helpers import pent_dense_apply
 
 GOLDEN = Path(__file__).with_name("golden") / "reference_pent.npz"
 

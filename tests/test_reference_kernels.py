@@ -16,7 +16,9 @@ import pytest
 
 import custen_gb300 as cs
 import oracle
-from tests.helpers import DeviceBuffer, field, sentinel, weights_for
+from custen_gb300.buffers import DeviceBuffer
+from custen_gb300.inputs import field, sentinel
+from tests.helpers import weights_for
 from tests.test_stencil_parity import FUN_IDS, geometry
 
 pytestmark = pytest.mark.gpu

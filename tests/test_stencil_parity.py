@@ -9,7 +9,9 @@ import pytest
 
 import custen_gb300 as cs
 import oracle
-from tests.helpers import DeviceBuffer, HostBuffer, field, sentinel, weights_for
+from custen_gb300.buffers import DeviceBuffer, HostBuffer
+from custen_gb300.inputs import field, sentinel
+from tests.helpers import weights_for
 
 pytestmark = pytest.mark.gpu
 

@@ -8,7 +8,8 @@ import pytest
 
 import custen_gb300 as cs
 import oracle
-from tests.helpers import DeviceBuffer, HostBuffer, weno_inputs
+from custen_gb300.buffers import DeviceBuffer, HostBuffer
+from custen_gb300.inputs import weno_inputs
 from tests.test_weno_oracle import weno_close
 
 pytestmark = pytest.mark.gpu

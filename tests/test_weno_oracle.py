@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
-from tests.helpers import weno_inputs
+from custen_gb300.inputs import weno_inputs
 
 GOLDEN = Path(__file__).with_name("golden") / "reference_weno.npz"
 
