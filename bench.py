@@ -299,7 +299,23 @@ def reference_gpu(args) -> dict:
             start = max(t, arr)
             t = start + k * t_of(m)
             ttc.append(t - arr)
+        # measured: the first grids of the batched list, one at a time for the full step count
+        sub = sizes[:args.plain_grids]
+        crng = np.random.default_rng(4)
+        t0 = time.perf_counter()
+        for m in sub:
+            r = oracle.ReferenceCahnHilliardGPU(crng.uniform(-0.1, 0.1, (m, m)))
+            r.step(args.ch_steps)
+            r.close()
+        sub_wall = time.perf_counter() - t0
+        sub_model = sum(step_s[m] * args.ch_steps for m in sub)
         out["ch_plain_loop"] = {
+            "measured_subset": {"grids": len(sub), "sizes": sub, "steps": args.ch_steps, "wall_s": round(sub_wall, 3),
+                                "steps_per_s": round(len(sub) * args.ch_steps / sub_wall, 1),
+                                "model_wall_s": round(sub_model, 3),
+                                "measured_over_model": round(sub_wall / sub_model, 3),
+                                "note": "the reference program run end to end on each grid (set-up, factorisation "
+                                        "and every step with its synchronisations), wall clock"},
             "step_ms_by_n": {str(m): round(v * 1e3, 4) for m, v in step_s.items()},
             "batched_config_steps_per_s": round(len(sizes) * args.ch_steps / total_b, 1),
             "served_config": {"makespan_s": round(t, 3), "steps_per_s": round(sum(served[2]) / t, 1),
@@ -390,12 +406,13 @@ def run_gpu(args, world, rank, local):
         f = f + (torch.rand((n, n), device=dev, dtype=torch.float64, generator=g) * 2e-3 - 1e-3)
         return f.to(dtype).contiguous()
 
-    def build_handles(dtype_t, cs_dtype, num_tiles=1, managed=False):
+    def build_handles(dtype_t, cs_dtype, num_tiles=1, managed=False, one_output=False):
         inp = make_field(dtype_t)
         outs, hs, keep = [], [], []
+        shared_out = torch.zeros((n, n), device=dev, dtype=dtype_t) if one_output else None
         for (nm, v, H, L, R, V, T, B, w, fun, _) in ops:
             wt = torch.tensor(w, device=dev, dtype=dtype_t)
-            o = torch.zeros((n, n), device=dev, dtype=dtype_t)
+            o = shared_out if one_output else torch.zeros((n, n), device=dev, dtype=dtype_t)
             func = cs.builtin_function(fun, cs_dtype) if fun >= 0 else None
             h = cs.Stencil(v, n, n, o, inp, wt, H=H, L=L, R=R, V=V, T=T, B=B, num_tiles=num_tiles, block_x=32,
                            block_y=8, dtype=cs_dtype, device=local, ncoef=len(w), func=func)
@@ -434,7 +451,7 @@ def run_gpu(args, world, rank, local):
         return total_ms, per_op, launches
 
     # ---- FP64 sweep (headline) ----
-    inp64, outs64, hs64, keep64 = build_handles(torch.float64, cs.F64)
+    inp64, outs64, hs64, keep64 = build_handles(torch.float64, cs.F64, one_output=args.one_output)
     sampler = ClockSampler(local)
     sampler.start()
     total_ms, per_op, launches = timed_sweep(hs64, args.steps, args.warmup)
@@ -483,7 +500,7 @@ def run_gpu(args, world, rank, local):
 
     # ---- FP32 precision variant: same sweep in FP32, error against the FP64 outputs ----
     fp32 = fp32_small = None
-    if not args.skip_fp32:
+    if not args.skip_fp32 and not args.one_output:   # the error needs every FP64 operator's own output
         fp32_small = run_precision(cs, torch, dev, 4096)
         inp32, outs32, hs32, keep32 = build_handles(torch.float32, cs.F32)
         ms32, per32, _ = timed_sweep(hs32, max(1, args.steps), 3)
@@ -514,6 +531,12 @@ def run_gpu(args, world, rank, local):
     pent = None
     if not args.skip_pent:
         pent = run_pent(cs, torch, dev, hbm_peak, batch=args.pent_batch)
+
+    # ---- e2e again, after the compute legs above: the spread between the two readings is the box's state
+    # (sustained GPU compute slows host<->device DMA afterwards), reported beside the first reading ----
+    e2e_after = None
+    if e2e is not None and not args.skip_e2e_after:
+        e2e_after = run_e2e(args, cs, np, local, ops, "pinned")
 
     # ---- CPU baseline (rank 0 only) ----
     cpu = None
@@ -589,6 +612,17 @@ def run_gpu(args, world, rank, local):
             line["fp32_4096"] = fp32_small
         if e2e is not None:
             line["e2e"] = e2e
+            if e2e_after is not None:
+                line["e2e"]["after_compute"] = {
+                    k: e2e_after[k] for k in ("value", "unit", "ms_per_step", "h2d_bytes_per_step", "d2h_bytes_per_step")}
+                if "link" in e2e_after:
+                    line["e2e"]["after_compute"]["link"] = {k: e2e_after["link"][k]
+                                                           for k in ("each_way_gbs", "link_each_way_gbs", "frac")}
+                line["e2e"]["spread"] = {
+                    "first": e2e["value"], "after_compute": e2e_after["value"],
+                    "note": "value is the reading taken first, before this process's compute legs; after_compute is "
+                            "the same leg after the FP64/FP32 sweeps, size sweep, WENO and pentadiagonal legs "
+                            "(about a minute of GPU compute)"}
         if e2e_managed is not None:
             line["e2e_managed"] = e2e_managed
         if cpu is not None:
@@ -956,19 +990,40 @@ def plain_step_seconds(cs, n: int, steps: int = 10) -> float:
     return dt
 
 
+def run_plain_loop(cs, sizes, steps):
+    """One grid at a time through this library, one step per launch sequence with a synchronisation after
+    every step (the structure of the reference's plain loop, cuPentCahnADI.cu:528-596), measured end to
+    end over the given grids in order. Returns the wall time in seconds."""
+    import numpy as np
+    crng = np.random.default_rng(4)
+    t0 = time.perf_counter()
+    for n in sizes:
+        b = cs.CahnHilliardBatch([n])
+        b.set_state(0, crng.uniform(-0.1, 0.1, (n, n)))
+        for _ in range(steps):
+            b.step(1, graph=False)
+            b.synchronize()
+        b.close()
+    return time.perf_counter() - t0
+
+
 def run_ch_batched(args, cs):
-    """512 periodic grids, N uniform over {64,...,1024} (seed 2), c0 ~ U(-0.1, 0.1), 500 steps."""
+    """512 periodic grids, N uniform over {64,...,1024} (seed 2), c0 ~ U(-0.1, 0.1), 500 steps; the FP64
+    batch and the FP32-stencil batch start from the same fields, and the FP32-stencil result is compared
+    with the FP64 one grid by grid."""
     import numpy as np
     rng = np.random.default_rng(2)
     sizes = [int(v) for v in rng.choice([64, 128, 256, 512, 1024], size=args.ch_sims)]
     steps = args.ch_steps
     out = {"config": f"{args.ch_sims} grids, N uniform over {{64..1024}} (seed 2), {steps} steps, lx = 2 pi, "
                      f"gamma 0.01, dt = 0.1 dx", "points": int(sum(n * n for n in sizes))}
+    finals = {}
     for label, dt in (("fp64", cs.F64), ("fp32_stencil", cs.F32)):
         b = cs.CahnHilliardBatch(sizes, rhs_dtype=dt)
         crng = np.random.default_rng(3)
         for k, n in enumerate(sizes):
             b.set_state(k, crng.uniform(-0.1, 0.1, (n, n)))
+        mean0 = [b.mean(k) for k in range(len(sizes))]
         b.step(2)
         b.synchronize()
         if args.ch_config >= 0:
@@ -984,27 +1039,56 @@ def run_ch_batched(args, cs):
         out[label] = {"wall_s": round(wall, 4), "steps_per_s": round(len(sizes) * steps / wall, 1),
                       "gpt_steps_per_s": round(out["points"] * steps / wall / 1e9, 3),
                       "ms_per_step": round(wall / steps * 1e3, 4), "launches": b.launches() - l0,
-                      "graphs": "pairs of steps", "kernel_config": cfg_name}
+                      "graphs": "pairs of steps", "kernel_config": cfg_name,
+                      "max_mass_drift": max(abs(b.mean(k) - mean0[k]) for k in range(len(sizes)))}
+        finals[label] = [b.state(k)[0] for k in range(len(sizes))]
         b.close()
-    # plain loop on the same GPU: one grid at a time (per-size step time measured, then summed)
+    # the FP32-stencil variant against the FP64 one (the pinned path: parity-tested against the oracle at
+    # these sizes), per grid size after 2 + steps steps from the same fields
+    err = {}
+    for k, n in enumerate(sizes):
+        a, r = finals["fp32_stencil"][k], finals["fp64"][k]
+        e = err.setdefault(str(n), {"grids": 0, "max_rel_l2": 0.0, "max_abs": 0.0})
+        e["grids"] += 1
+        e["max_rel_l2"] = max(e["max_rel_l2"], float(np.linalg.norm(a - r) / np.linalg.norm(r)))
+        e["max_abs"] = max(e["max_abs"], float(np.abs(a - r).max()))
+    del finals
+    out["fp32_stencil"]["error_vs_fp64"] = {
+        "by_n": err, "steps": steps + 2,
+        "note": "relative L2 and max abs of each FP32-stencil grid against the same grid in FP64 (same c0, same "
+                "step count), maxima per grid size; max_mass_drift: |mean(c_end) - mean(c0)|, FP64 compensated "
+                "sums on the device"}
+    # plain loop on the same GPU: one grid at a time, measured on the first grids of the list, beside the
+    # per-size model used for the whole list
     per_size = {n: plain_step_seconds(cs, n) for n in sorted(set(sizes))}
     plain_total = sum(per_size[n] * steps for n in sizes)
+    sub = sizes[:args.plain_grids]
+    sub_wall = run_plain_loop(cs, sub, steps)
+    sub_model = sum(per_size[n] * steps for n in sub)
     out["plain_loop"] = {"steps_per_s": round(len(sizes) * steps / plain_total, 1),
                          "wall_s_estimated": round(plain_total, 3),
                          "step_ms_by_n": {str(n): round(v * 1e3, 4) for n, v in per_size.items()},
                          "method": "this library's kernels, one grid per launch sequence, synchronised per "
-                                   "step; per-size step time x steps, summed over grids"}
+                                   "step; per-size step time x steps, summed over grids",
+                         "measured_subset": {
+                             "grids": len(sub), "sizes": sub, "steps": steps, "wall_s": round(sub_wall, 3),
+                             "steps_per_s": round(len(sub) * steps / sub_wall, 1),
+                             "model_wall_s": round(sub_model, 3), "measured_over_model": round(sub_wall / sub_model, 3),
+                             "note": "the first grids of the list run one at a time for the full step count, each "
+                                     "step synchronised, wall clock end to end (grid set-up included)"}}
     out["speedup_vs_plain_loop"] = round(out["fp64"]["steps_per_s"] / out["plain_loop"]["steps_per_s"], 2)
+    out["speedup_vs_plain_loop_measured"] = round(
+        out["fp64"]["steps_per_s"] / out["plain_loop"]["measured_subset"]["steps_per_s"], 2)
     return out
 
 
-def served_workload(args):
+def served_workload(args, rate=None, count=None, seed=3):
     """(arrival times, grid sizes, step counts) of the served request stream: Poisson arrivals (mean rate,
     seed 3), N log-uniform 128-2048 rounded to a multiple of 32, steps U(100, 5000)."""
     import numpy as np
-    rng = np.random.default_rng(3)
-    R = args.served_requests
-    gaps = rng.exponential(1.0 / args.served_rate, size=R)
+    rng = np.random.default_rng(seed)
+    R = count or args.served_requests
+    gaps = rng.exponential(1.0 / (rate or args.served_rate), size=R)
     arrivals = [float(a) for a in np.cumsum(gaps) - gaps[0]]
     sizes = [int(max(128, min(2048, round(math.exp(v) / 32) * 32)))
              for v in rng.uniform(math.log(128), math.log(2048), size=R)]
@@ -1012,41 +1096,69 @@ def served_workload(args):
     return arrivals, sizes, steps
 
 
-def run_ch_served(args, cs):
-    """Poisson arrivals (mean rate, seed 3), N log-uniform 128-2048 rounded to 32, steps U(100, 5000),
-    c0 ~ U(-0.1, 0.1), HBM budget 150 GB, a fixed number of requests."""
+def serve(args, cs, arrivals, sizes, steps):
+    """Run one request stream through the server; its figures."""
     import numpy as np
-    R = args.served_requests
-    arrivals, sizes, steps = served_workload(args)
+    R = len(sizes)
     srv = cs.CahnHilliardServer(hbm_budget_bytes=150e9, chunk_steps=args.served_chunk, keep_results=False)
     for k in range(R):
         srv.submit(sizes[k], steps[k], arrival=float(arrivals[k]), seed=1000 + k)
     srv.run()
     st = srv.stats()
-    ttc = np.array([srv.result(k, field=False)["ttc"] for k in range(R)])
-    drift = max(abs(srv.result(k, field=False)["mean_end"] - srv.result(k, field=False)["mean0"]) for k in range(R))
+    res = [srv.result(k, field=False) for k in range(R)]
     srv.close()
+    ttc = np.array([r["ttc"] for r in res])
+    wait = np.array([r["admit"] - r["arrival"] for r in res])
+    drift = max(abs(r["mean_end"] - r["mean0"]) for r in res)
     total_steps = int(sum(steps))
-    out = {"config": f"{R} requests, Poisson {args.served_rate}/s (seed 3), N log-uniform 128-2048 (multiples of "
-                     f"32), steps U(100, 5000), budget 150 GB, chunk {args.served_chunk} steps",
-           "makespan_s": round(st["makespan"], 3), "steps_per_s": round(total_steps / st["makespan"], 1),
-           "gpt_steps_per_s": round(st["point_steps"] / st["makespan"] / 1e9, 3),
-           "ttc_p50_s": round(float(np.percentile(ttc, 50)), 3), "ttc_p99_s": round(float(np.percentile(ttc, 99)), 3),
-           "max_resident": st["max_active"], "peak_resident_gb": round(st["peak_bytes"] / 1e9, 2),
-           "max_mass_drift": drift}
-    # the plain sequential loop: first come first served, one grid at a time
-    per_size = {n: plain_step_seconds(cs, n, steps=5) for n in sorted(set(sizes))}
-    t = 0.0
-    ttc_p = []
-    for k in range(R):
-        start = max(t, float(arrivals[k]))
-        t = start + steps[k] * per_size[sizes[k]]
-        ttc_p.append(t - float(arrivals[k]))
-    out["plain_loop"] = {"makespan_s": round(t, 3), "steps_per_s": round(total_steps / t, 1),
-                         "ttc_p50_s": round(float(np.percentile(ttc_p, 50)), 3),
-                         "ttc_p99_s": round(float(np.percentile(ttc_p, 99)), 3),
-                         "method": "FCFS queue over the measured per-size step time of one grid at a time"}
+    return {"requests": R, "makespan_s": round(st["makespan"], 3),
+            "arrivals_span_s": round(float(arrivals[-1]), 3),
+            "arrivals_span_over_makespan": round(float(arrivals[-1]) / st["makespan"], 3),
+            "steps_per_s": round(total_steps / st["makespan"], 1),
+            "gpt_steps_per_s": round(st["point_steps"] / st["makespan"] / 1e9, 3),
+            "ttc_p50_s": round(float(np.percentile(ttc, 50)), 3), "ttc_p99_s": round(float(np.percentile(ttc, 99)), 3),
+            "admission_wait_p50_s": round(float(np.percentile(wait, 50)), 4),
+            "admission_wait_p99_s": round(float(np.percentile(wait, 99)), 4),
+            "max_resident": st["max_active"], "peak_resident_gb": round(st["peak_bytes"] / 1e9, 2),
+            "max_mass_drift": drift}
+
+
+def fcfs_plain(per_size, arrivals, sizes, steps):
+    """The plain sequential loop over a request stream: first come first served, one grid at a time."""
+    import numpy as np
+    t, ttc = 0.0, []
+    for a, n, k in zip(arrivals, sizes, steps):
+        start = max(t, float(a))
+        t = start + k * per_size[n]
+        ttc.append(t - float(a))
+    return {"makespan_s": round(t, 3), "steps_per_s": round(int(sum(steps)) / t, 1),
+            "ttc_p50_s": round(float(np.percentile(ttc, 50)), 3), "ttc_p99_s": round(float(np.percentile(ttc, 99)), 3),
+            "method": "FCFS queue over the measured per-size step time of one grid at a time"}
+
+
+def run_ch_served(args, cs):
+    """Poisson arrivals (mean rate, seed 3), N log-uniform 128-2048 rounded to 32, steps U(100, 5000),
+    c0 ~ U(-0.1, 0.1), HBM budget 150 GB, a fixed number of requests.
+
+    At the configured 200 requests/s the offered load is far above what one GPU serves, so every request
+    arrives within the first fraction of a second and the run drains a full queue. A second stream at 0.9 of
+    the throughput measured on the first (same size and step distributions, seed 4) keeps requests arriving
+    while others complete, so admission happens continuously over the whole run."""
+    arrivals, sizes, steps = served_workload(args)
+    out = serve(args, cs, arrivals, sizes, steps)
+    out["config"] = (f"{len(sizes)} requests, Poisson {args.served_rate}/s (seed 3), N log-uniform 128-2048 "
+                     f"(multiples of 32), steps U(100, 5000), budget 150 GB, chunk {args.served_chunk} steps")
+    rate = 0.9 * len(sizes) / out["makespan_s"]
+    c_arr, c_sizes, c_steps = served_workload(args, rate=rate, count=args.served_continuous, seed=4)
+    cont = serve(args, cs, c_arr, c_sizes, c_steps)
+    cont["config"] = (f"{len(c_sizes)} requests, Poisson {rate:.2f}/s (0.9 x the requests/s served above; seed 4), "
+                      f"same N and step distributions, budget 150 GB, chunk {args.served_chunk} steps")
+    per_size = {n: plain_step_seconds(cs, n, steps=5) for n in sorted(set(sizes) | set(c_sizes))}
+    out["plain_loop"] = fcfs_plain(per_size, arrivals, sizes, steps)
     out["speedup_vs_plain_loop"] = round(out["steps_per_s"] / out["plain_loop"]["steps_per_s"], 2)
+    cont["plain_loop"] = fcfs_plain(per_size, c_arr, c_sizes, c_steps)
+    cont["speedup_vs_plain_loop"] = round(cont["steps_per_s"] / cont["plain_loop"]["steps_per_s"], 2)
+    out["continuous"] = cont
     return out
 
 
@@ -1063,6 +1175,7 @@ def main():
     ap.add_argument("--skip-fp32", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-e2e-managed", action="store_true")
+    ap.add_argument("--skip-e2e-after", action="store_true", help="skip the second e2e reading after the compute legs")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-ch", action="store_true")
     ap.add_argument("--skip-served", action="store_true")
@@ -1071,10 +1184,17 @@ def main():
     ap.add_argument("--served-requests", type=int, default=96)
     ap.add_argument("--served-rate", type=float, default=200.0)
     ap.add_argument("--served-chunk", type=int, default=16)
+    ap.add_argument("--served-continuous", type=int, default=48,
+                    help="requests of the second served stream (arrivals at 0.9 x the measured throughput)")
+    ap.add_argument("--plain-grids", type=int, default=32,
+                    help="grids of the batched workload run one at a time for the measured plain loop")
     ap.add_argument("--skip-ref-gpu", action="store_true")
     ap.add_argument("--skip-sizes", action="store_true")
     ap.add_argument("--skip-weno", action="store_true")
     ap.add_argument("--skip-indirect", action="store_true")
+    ap.add_argument("--one-output", action="store_true",
+                    help="the FP64 sweep's operators all write one output field (4 GiB on the device at 16384^2 "
+                         "instead of 26; the same work and DRAM traffic per launch)")
     ap.add_argument("--skip-pent", action="store_true")
     ap.add_argument("--pent-batch", type=int, default=1 << 18, help="systems in the pentadiagonal leg (256 unknowns each)")
     ap.add_argument("--ch-config", type=int, default=-1,

@@ -48,8 +48,9 @@ namespace ch {
 // ------------------------------------------------------------------------------------------------
 // K1: right-hand side
 // ------------------------------------------------------------------------------------------------
-// T = double: FP64 arithmetic; T = float: the FP32 precision variant (inputs and coefficients rounded
-// to float, result widened back to double for the FP64 solve).
+// T = double: FP64 arithmetic; T = float: the FP32 precision variant (cBar, c^3 - c, the inner Laplacian
+// and h in FP32 from inputs and coefficients rounded to float; the outer Laplacian of the FP32 h values
+// and the time-derivative term summed in FP64, which keeps the mass conserved to FP64 rounding).
 //
 // The reference's two explicit stencils are the 13-point biharmonic sigma_lin * [-1; -2 8 -2; -1 8 -20
 // 8 -1; ...] on cBar and the 5-point Laplacian sigma_nl * [1; 1 -4 1; 1] on c^3 - c
@@ -72,15 +73,16 @@ template <typename T, int NW>
 __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restrict__ grids,
                                                           const Item* __restrict__ items, int n_items, int parity,
                                                           unsigned int* counter) {
-    __shared__ T cb[36][37];   // cBar over the block and a 2-point halo
-    __shared__ T hh[34][35];   // sigma_nl * (c^3 - c), then h, over the block and a 1-point halo
-    __shared__ T dco[32][33];  // cCurr - cOld at the block's points
+    __shared__ T cb[36][37];        // cBar over the block and a 2-point halo
+    __shared__ T hh[34][35];        // sigma_nl * (c^3 - c), then h, over the block and a 1-point halo
+    __shared__ double dco[32][33];  // cCurr - cOld at the block's points (FP64 in both variants)
     __shared__ int s_item;
     constexpr int NT = NW * BLK;
     const int tid = threadIdx.x;
     const int lane = tid & (BLK - 1), warp = tid / BLK;
     const volatile double* factors = g_rhs_factors;
-    const T two = (T)factors[0], m_four = (T)factors[1], m_two_thirds = (T)factors[2];
+    const T two = (T)factors[0], m_four = (T)factors[1];
+    const double m_four_d = factors[1], m_two_thirds_d = factors[2];
     for (;;) {
         if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
         __syncthreads();
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
             const T c32 = (T)cv, o32 = (T)ov;
             cb[r][c] = fma(two, c32, -o32);
             if (r >= 1 && r < 35 && c >= 1 && c < 35) hh[r - 1][c - 1] = s_nl * fma(c32 * c32, c32, -c32);
-            if (r >= 2 && r < 34 && c >= 2 && c < 34) dco[r - 2][c - 2] = c32 - o32;
+            if (r >= 2 && r < 34 && c >= 2 && c < 34) dco[r - 2][c - 2] = cv - ov;
         }
         __syncthreads();
         // h = sigma_nl * g - sigma_lin * Lap(cBar) over the 34 x 34 block + halo
@@ -123,14 +125,19 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
             hh[r][c] = fma(-s_lin, lap, hh[r][c]);
         }
         __syncthreads();
-        // rhs = Lap(h) - (2/3)(cCurr - cOld)  (findRHS, cuPentCahnADI.cu:72-86); lane = column
+        // rhs = Lap(h) - (2/3)(cCurr - cOld)  (findRHS, cuPentCahnADI.cu:72-86); lane = column. Summed in
+        // FP64 in both variants: over FP32 values of h (the precision variant) the FP64 sums are exact, so
+        // the discrete Laplacian sums to zero over the periodic grid and the mass is conserved to FP64
+        // rounding, as in the FP64 variant.
         const int j = lane;
         double* out = gd.tmp + (size_t)y0 * n + x0 + j;
 #pragma unroll 4
         for (int rr = warp; rr < BLK; rr += NW) {
-            const T lap = fma(m_four, hh[rr + 1][j + 1], (hh[rr][j + 1] + hh[rr + 2][j + 1]) + (hh[rr + 1][j] + hh[rr + 1][j + 2]));
+            const double lap = fma(m_four_d, (double)hh[rr + 1][j + 1],
+                                   ((double)hh[rr][j + 1] + (double)hh[rr + 2][j + 1]) +
+                                       ((double)hh[rr + 1][j] + (double)hh[rr + 1][j + 2]));
             if (!in_bounds((long long)(y0 + rr) * n + x0 + j, 0, (long long)n * n)) continue;
-            out[(size_t)rr * n] = (double)fma(m_two_thirds, dco[rr][j], lap);
+            out[(size_t)rr * n] = fma(m_two_thirds_d, dco[rr][j], lap);
         }
         __syncthreads();
     }
@@ -1144,16 +1151,18 @@ void config_name(const ChConfig& c, char* name, size_t len) {
         snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
 }
 
-// the two passes of the split right-hand side; pass 2 claims work through the step's fourth counter
+// The two passes of the split right-hand side; pass 2 claims work through the step's fourth counter.
+// Pass 2 runs in FP64 in both variants: the precision variant's h buffer holds FP32 values, whose FP64
+// Laplacian is exact, so its mass is conserved to FP64 rounding (the one-pass kernel does the same).
 template <typename T>
 static void launch_rhs2(int nw, int grid, const GridDev* g, const Item* it, int n, int parity, unsigned int* ctr,
                         cudaStream_t s) {
     if (nw == 4) {
         ch_h_kernel<T, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr);
-        ch_rhs2_kernel<T, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
+        ch_rhs2_kernel<double, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
     } else {
         ch_h_kernel<T, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr);
-        ch_rhs2_kernel<T, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
+        ch_rhs2_kernel<double, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
     }
 }
 

