@@ -32,9 +32,10 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# ncu DRAM bytes (read + write) per stencil launch, mean over the 12 operators of the sweep at 6144^2
-# (profiles/stencil_sweep_traffic.md); the field is streamed once per launch, so it scales with n^2.
-TRAFFIC_6144 = 559918997.0
+# ncu DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per stencil launch: the mean over the 12
+# launches of one timed sweep at 16384^2 (FP64, L2 not flushed between launches), 1.032 x the algorithmic
+# 16 B per point. Other sizes scale it by the point count: every launch streams its field once.
+TRAFFIC_16384 = 4431034304.0
 
 def operators(n: int):
     """(name, variant, H, L, R, V, T, B, weights, fun_id, dfma_per_point) of the 12-operator sweep."""
@@ -587,9 +588,10 @@ def run_gpu(args, world, rank, local):
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
                          "frac": round(achieved_gbs / hbm_peak, 4),
-                         "traffic": args.traffic if args.traffic is not None else round(TRAFFIC_6144 * (n / 6144) ** 2),
+                         "traffic": args.traffic if args.traffic is not None else round(TRAFFIC_16384 * (n / 16384) ** 2),
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, mean of the "
-                                           "12 operators at 6144^2, scaled by the point count",
+                                           "12 operators of one timed sweep at 16384^2" +
+                                           ("" if n == 16384 else ", scaled by the point count"),
                          "peak_source": f"{hbm_src} hbm_gbs",
                          "note": "16 B/pt algorithmic; FP64 kernels are bound by the FP64 FMA pipe (binding): at "
                                  "the measured FP64 FMA rate the sweep's operators cap at 1.4-2.5 TB/s",
@@ -1043,21 +1045,42 @@ def run_ch_batched(args, cs):
                       "max_mass_drift": max(abs(b.mean(k) - mean0[k]) for k in range(len(sizes)))}
         finals[label] = [b.state(k)[0] for k in range(len(sizes))]
         b.close()
+    # conditioning of the problem: FP64 from c0 rounded to FP32 (a perturbation of FP32 rounding size), the
+    # same step count; phase separation amplifies any perturbation, so this is the yardstick for the
+    # FP32-stencil error above
+    b = cs.CahnHilliardBatch(sizes)
+    crng = np.random.default_rng(3)
+    for k, n in enumerate(sizes):
+        b.set_state(k, crng.uniform(-0.1, 0.1, (n, n)).astype(np.float32).astype(np.float64))
+    b.set_config(args.ch_config if args.ch_config >= 0 else 17)
+    b.step(2 + steps)
+    b.synchronize()
+    finals["fp64_c0_fp32"] = [b.state(k)[0] for k in range(len(sizes))]
+    b.close()
     # the FP32-stencil variant against the FP64 one (the pinned path: parity-tested against the oracle at
     # these sizes), per grid size after 2 + steps steps from the same fields
     err = {}
     for k, n in enumerate(sizes):
-        a, r = finals["fp32_stencil"][k], finals["fp64"][k]
-        e = err.setdefault(str(n), {"grids": 0, "max_rel_l2": 0.0, "max_abs": 0.0})
+        r = finals["fp64"][k]
+        a, p = finals["fp32_stencil"][k], finals["fp64_c0_fp32"][k]
+        e = err.setdefault(str(n), {"grids": 0, "max_rel_l2": 0.0, "median_rel_l2": [], "max_abs": 0.0,
+                                    "fp64_c0_fp32_max_rel_l2": 0.0})
         e["grids"] += 1
-        e["max_rel_l2"] = max(e["max_rel_l2"], float(np.linalg.norm(a - r) / np.linalg.norm(r)))
+        rl = float(np.linalg.norm(a - r) / np.linalg.norm(r))
+        e["max_rel_l2"] = max(e["max_rel_l2"], rl)
+        e["median_rel_l2"].append(rl)
         e["max_abs"] = max(e["max_abs"], float(np.abs(a - r).max()))
+        e["fp64_c0_fp32_max_rel_l2"] = max(e["fp64_c0_fp32_max_rel_l2"], float(np.linalg.norm(p - r) / np.linalg.norm(r)))
+    for e in err.values():
+        e["median_rel_l2"] = float(np.median(e["median_rel_l2"]))
     del finals
     out["fp32_stencil"]["error_vs_fp64"] = {
-        "by_n": err, "steps": steps + 2,
+        "by_n": dict(sorted(err.items(), key=lambda kv: int(kv[0]))), "steps": steps + 2,
         "note": "relative L2 and max abs of each FP32-stencil grid against the same grid in FP64 (same c0, same "
-                "step count), maxima per grid size; max_mass_drift: |mean(c_end) - mean(c0)|, FP64 compensated "
-                "sums on the device"}
+                "step count), maxima (and median rel L2) per grid size. fp64_c0_fp32_max_rel_l2: FP64 run from c0 "
+                "rounded to FP32 against the FP64 run, the problem's own amplification of a perturbation of that "
+                "size over these steps. max_mass_drift: |mean(c_end) - mean(c0)|, FP64 compensated sums on the "
+                "device"}
     # plain loop on the same GPU: one grid at a time, measured on the first grids of the list, beside the
     # per-size model used for the whole list
     per_size = {n: plain_step_seconds(cs, n) for n in sorted(set(sizes))}
@@ -1204,8 +1227,8 @@ def main():
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],
                     help="kernel configuration choice: 0 defaults, 1 tune at the first Compute (default), 2 always")
     ap.add_argument("--traffic", type=float, default=None,
-                    help="dram bytes per launch from an ncu capture (default: the 6144^2 capture in "
-                         "profiles/stencil_sweep_traffic.md scaled to --n)")
+                    help="dram bytes per launch from an ncu capture (default: the 16384^2 capture of the "
+                         "sweep, scaled to --n by the point count)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
