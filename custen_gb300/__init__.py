@@ -73,6 +73,7 @@ def lib() -> ctypes.CDLL:
         L.custen_builtin_fun_id.argtypes = [vp, i]
         L.custen_device_error.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
         L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
+        L.custen_create_slab.argtypes = [vp, i, i, i, i, i, i, i, i, i, vp, vp, vp, vp, vp, i, i, i, i, i, i, i, vp]
         L.custen_create_2d_xyweno_adv_p.argtypes = [vp, i, i, i, i, i, i, ctypes.c_double, ctypes.c_double, vp, vp,
                                                     vp, vp]
         L.custen_compute.argtypes = [vp, i]

@@ -142,6 +142,9 @@ struct PlanPrivate {
     void* fused_func;
     int fused_pre;
     int cfg;   // kernel configuration (stencil_configs.h) of the device-resident launches; -1 not chosen yet
+    // Slab handles (custen_create_slab): the handle's one tile is tile `slab` of a field of `slabs` tiles
+    // held by several owners; its halo rows are the caller's buffers. slabs = 0: an ordinary handle.
+    int slab, slabs;
     // Host-resident fields (pinned or system memory) are streamed through device staging slots:
     // kStageSlots slots of (T + chunk + B) input rows and chunk output rows, plus the weights.
     // Allocated at the first such Compute, freed by Destroy.

@@ -176,6 +176,8 @@ int create_plan(cuSten_t* h, int variant, int dtype, int dev, int numTiles, int 
     p.stage_slot_bytes = 0;
     p.stage_rows = 0;
     p.stage_events_ready = 0;
+    p.slab = 0;
+    p.slabs = 0;
 
     const int esz = dtype == DT_F64 ? 8 : 4;
     const int dir = variant_dir(variant);
@@ -302,8 +304,9 @@ static int swap_plan(cuSten_t* h, void* newInput) {
     }
     // X variants ignore the argument (custenCreateDestroy2DXp.cu:179-190); Y and XY variants
     // recompute every halo pointer from it with the periodic formulas, Ynp included
-    // (custenCreateDestroy2DYnp.cu:248-282).
-    if (variant_dir(p->variant) != 0) {
+    // (custenCreateDestroy2DYnp.cu:248-282). Slab handles keep their halo buffers (the exchange fills
+    // them before each Compute) and ignore the argument.
+    if (variant_dir(p->variant) != 0 && !p->slabs) {
         if (newInput == nullptr) return fail_arg("Swap needs the new input pointer for Y/XY stencils");
         set_halos_periodic(h, newInput, p->dtype == DT_F64 ? 8 : 4);
     }
@@ -586,7 +589,10 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
     a.bx = h->BLOCK_X;
     a.by = h->BLOCK_Y;
     a.nyTile = nyT;
-    a.numTiles = nt;
+    // a slab handle's tile is tile p->slab of p->slabs: the write rules and the halo rule take the
+    // field-wide tile numbering, rows are numbered from the field's first row
+    const int tile0 = p->slabs ? p->slab : 0, tiles_all = p->slabs ? p->slabs : nt;
+    a.numTiles = tiles_all;
     a.wrap_x = periodic && dir != 1;
     if (variant_is_fun(p->variant) && g_fun_fusion.load(std::memory_order_relaxed)) {
         // The library's own c^3 - c functions (ids 1, 3, 5) with the window they read: cube each staged
@@ -640,17 +646,18 @@ int compute_plan(cuSten_t* h, int offload, cudaStream_t* explicit_stream) {
             a.v = h->vVel[t_first];
         }
         a.rows = t_count * nyT;
-        a.row0 = t_first * nyT;
+        a.row0 = (tile0 + t_first) * nyT;
         const int t_last = t_first + t_count - 1;
         a.top = (dir != 0) ? (const void*)h->boundaryTop[t_first] : nullptr;
         a.bot = (dir != 0) ? (const void*)h->boundaryBottom[t_last] : nullptr;
-        a.has_top = (dir != 0 && p->T > 0) && (periodic || t_first > 0);
-        a.has_bot = (dir != 0 && p->B > 0) && (periodic || t_last < nt - 1);
+        a.has_top = (dir != 0 && p->T > 0) && (periodic || tile0 + t_first > 0);
+        a.has_bot = (dir != 0 && p->B > 0) && (periodic || tile0 + t_last < tiles_all - 1);
         a.vec_ok = row_aligned && aligned16(a.in) && aligned16(a.out) && (!a.has_top || aligned16(a.top)) &&
                    (!a.has_bot || aligned16(a.bot));
     };
 
     if (kind == 2 || kind_out == 2) {
+        if (p->slabs) return fail_arg("slab handles take device or managed memory");
         // Pinned or system memory: stream the rows through device staging slots.
         cudaStream_t s_out = explicit_stream ? *explicit_stream
                                              : (p->use_user_stream ? p->user_stream : h->streams[2]);
@@ -896,6 +903,35 @@ int custen_create(cuSten_t* h, int variant, int dtype, int dev, int nt, int nx, 
     const int field = dir == 2 ? H * V : (dir == 0 ? H : V);
     return create_plan(h, variant, dtype, dev, nt, nx, ny, bx, by, out, in, coef, H, L, R, V, T, B, ncoef, func,
                        field);
+}
+int custen_create_slab(cuSten_t* h, int variant, int dtype, int dev, int slab, int num_slabs, int nx, int ny_slab,
+                       int bx, int by, void* out, void* in, void* halo_top, void* halo_bottom, void* coef, int H, int L,
+                       int R, int V, int T, int B, int ncoef, void* func) {
+    if (variant == V_XYWENOADVP) return fail_arg("slab handles take the twelve weighted / Fun variants");
+    if (num_slabs < 1 || slab < 0 || slab >= num_slabs)
+        return fail_arg("slab %d of %d: the index must lie in [0, num_slabs)", slab, num_slabs);
+    if (ny_slab < 1 || (long long)ny_slab * num_slabs > (1ll << 31) - 1) return fail_arg("slab rows out of range");
+    const int dir = (variant >= 0 && variant < V_COUNT) ? variant_dir(variant) : 0;
+    const bool periodic = variant >= 0 && variant < V_COUNT && variant_is_periodic(variant);
+    if (dir != 0) {
+        if (T > 0 && (periodic || slab > 0) && halo_top == nullptr)
+            return fail_arg("slab %d reads %d halo rows above it: halo_top is NULL", slab, T);
+        if (B > 0 && (periodic || slab < num_slabs - 1) && halo_bottom == nullptr)
+            return fail_arg("slab %d reads %d halo rows below it: halo_bottom is NULL", slab, B);
+    }
+    const int field = dir == 2 ? H * V : (dir == 0 ? H : V);
+    int st = create_plan(h, variant, dtype, dev, 1, nx, ny_slab, bx, by, out, in, coef, H, L, R, V, T, B, ncoef, func,
+                         field);
+    if (st != ST_OK) return st;
+    PlanPrivate* p = priv_of(h);
+    p->slab = slab;
+    p->slabs = num_slabs;
+    h->ny = ny_slab * num_slabs;
+    if (dir != 0) {
+        h->boundaryTop[0] = static_cast<double*>(halo_top);
+        h->boundaryBottom[0] = static_cast<double*>(halo_bottom);
+    }
+    return ST_OK;
 }
 int custen_compute(cuSten_t* h, int offload) { return compute_plan(h, offload, nullptr); }
 int custen_compute_on_stream(cuSten_t* h, int offload, void* stream) {

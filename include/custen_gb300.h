@@ -78,6 +78,19 @@ int custen_builtin_fun_id(const void* f, int dtype);
 int custen_create(cuSten_t* h, int variant, int dtype, int deviceNum, int numTiles, int nx, int ny, int BLOCK_X,
                   int BLOCK_Y, void* dataOutput, void* dataInput, void* coef, int H, int L, int R, int V, int T,
                   int B, int ncoef, void* func);
+/* A handle over one y-slab of a field split across several owners (processes, GPUs): the slab is tile
+ * `slab` of `num_slabs` tiles of ny_slab rows each, the numTiles layout of the reference
+ * (custenCreateDestroy2DYp.cu:182-216) with each tile in its own allocation. halo_top holds the T rows above
+ * the slab and halo_bottom the B rows below it (periodic variants wrap around the field); the caller fills
+ * them before each Compute, e.g. from the neighbouring slabs' edge rows (custen_gb300.slabs). Either may be
+ * NULL where the variant never reads it (non-periodic variants: above slab 0, below the last slab). The
+ * non-periodic write rules are those of tile `slab` of the whole field, so the slabs together give exactly
+ * the single-handle result with numTiles = num_slabs. Swap exchanges in and out and keeps the halo buffers.
+ * Device or managed memory. */
+int custen_create_slab(cuSten_t* h, int variant, int dtype, int deviceNum, int slab, int num_slabs, int nx,
+                       int ny_slab, int BLOCK_X, int BLOCK_Y, void* dataOutput, void* dataInput, void* halo_top,
+                       void* halo_bottom, void* coef, int H, int L, int R, int V, int T, int B, int ncoef,
+                       void* func);
 int custen_compute(cuSten_t* h, int offload);                       /* cuStenCompute2D*(h, offload) */
 int custen_compute_on_stream(cuSten_t* h, int offload, void* stream); /* same, all work on `stream` */
 int custen_swap(cuSten_t* h, void* dataInput);                      /* cuStenSwap2D*(h, dataInput) */
