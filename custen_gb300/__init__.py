@@ -73,6 +73,7 @@ def lib() -> ctypes.CDLL:
         L.custen_builtin_fun_id.argtypes = [vp, i]
         L.custen_device_error.argtypes = [ctypes.POINTER(ctypes.c_uint), i]
         L.custen_create.argtypes = [vp, i, i, i, i, i, i, i, i, vp, vp, vp, i, i, i, i, i, i, i, vp]
+        L.custen_compute_group.argtypes = [ctypes.POINTER(ctypes.c_void_p), i, i, vp]
         L.custen_create_slab.argtypes = [vp, i, i, i, i, i, i, i, i, i, vp, vp, vp, vp, vp, i, i, i, i, i, i, i, vp]
         L.custen_create_2d_xyweno_adv_p.argtypes = [vp, i, i, i, i, i, i, ctypes.c_double, ctypes.c_double, vp, vp,
                                                     vp, vp]
@@ -209,6 +210,15 @@ def tune_cache_path() -> str:
 def set_fun_fusion(enable: bool) -> None:
     """Fused path for the library's own c^3 - c Fun functions (default on); off = indirect calls."""
     lib().custen_set_fun_fusion(int(bool(enable)))
+
+
+def compute_group(stencils, offload: int = 0, stream=None) -> None:
+    """One Compute of each of several independent handles (custen_compute_group), free to overlap on the
+    GPU; ordered after the work queued on `stream` (a torch stream, a raw handle or None) and before work
+    queued there later."""
+    arr = (ctypes.c_void_p * len(stencils))(*[ctypes.addressof(st.handle) for st in stencils])
+    s = 0 if stream is None else (stream if isinstance(stream, int) else int(stream.cuda_stream))
+    _check(lib().custen_compute_group(arr, len(stencils), offload, s))
 
 
 def set_max_ctas(max_ctas: int) -> None:

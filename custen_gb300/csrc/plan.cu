@@ -934,6 +934,33 @@ int custen_create_slab(cuSten_t* h, int variant, int dtype, int dev, int slab, i
     return ST_OK;
 }
 int custen_compute(cuSten_t* h, int offload) { return compute_plan(h, offload, nullptr); }
+int custen_compute_group(cuSten_t* const* handles, int count, int offload, void* stream) {
+    if (count < 0 || (count > 0 && handles == nullptr)) return fail_arg("custen_compute_group: no handles");
+    for (int k = 0; k < count; ++k) {
+        if (!priv_of(handles[k])) return fail_arg("custen_compute_group: handle %d was not created by this library", k);
+        for (int j = 0; j < k; ++j)
+            if (handles[j] == handles[k]) return fail_arg("custen_compute_group: handle %d appears twice", k);
+    }
+    if (count == 0) return ST_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CU_TRY(cudaSetDevice(handles[0]->deviceNum), "Setting current device");
+    // fork: every handle's first stream follows the work already queued on `stream`
+    CU_TRY(cudaEventRecord(handles[0]->events[1], s), "Recording the group's fork event");
+    for (int k = 0; k < count; ++k)
+        CU_TRY(cudaStreamWaitEvent(handles[k]->streams[0], handles[0]->events[1], 0), "Ordering a group member");
+    // each handle's Compute, all of its work on its own first stream
+    for (int k = 0; k < count; ++k) {
+        cudaStream_t hs = handles[k]->streams[0];
+        const int st = compute_plan(handles[k], offload, &hs);
+        if (st != ST_OK) return st;
+    }
+    // join: later work on `stream` follows every member
+    for (int k = 0; k < count; ++k) {
+        CU_TRY(cudaEventRecord(handles[k]->events[0], handles[k]->streams[0]), "Recording a group member's end");
+        CU_TRY(cudaStreamWaitEvent(s, handles[k]->events[0], 0), "Joining the group");
+    }
+    return ST_OK;
+}
 int custen_compute_on_stream(cuSten_t* h, int offload, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     return compute_plan(h, offload, &s);
