@@ -584,7 +584,8 @@ def run_gpu(args, world, rank, local):
             "data": "synthetic: sin(3x)cos(5y)+U(-1e-3,1e-3), seed 1",
             "config": {"workload": f"cuSten stencil sweep FP64 {n}^2: 12 operators (X/Y 5-pt p/np, XY 3x3 "
                                    f"cross p/np, Fun c^3-c X/Y/XY p/np), numTiles=1, device-resident",
-                       "nx": n, "ny": n, "numTiles": 1, "l2": "inputs larger than L2 (2 GiB per field)",
+                       "nx": n, "ny": n, "numTiles": 1, "l2": f"inputs larger than L2 ({n * n * 8 / 2**30:.3g} GiB per field)" if n * n * 8 > 129e6
+                       else f"field of {n * n * 8 / 2**20:.3g} MiB fits in L2 (not the headline size)",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
                          "frac": round(achieved_gbs / hbm_peak, 4),
