@@ -82,3 +82,19 @@ def test_errors_are_status_codes_not_exits(built):
     assert b"divisible by numTiles" in cs.lib().custen_last_error()
     rc = cs.lib().custen_compute(h, 0)
     assert rc == 2 and b"not created" in cs.lib().custen_last_error()
+
+
+def test_group_and_slab_argument_errors(built):
+    """Argument checks of custen_compute_group and custen_create_slab run before any device work."""
+    L = cs.lib()
+    assert L.custen_compute_group(None, 0, 0, None) == 0
+    assert L.custen_compute_group(None, -1, 0, None) == 2
+    stale = ctypes.create_string_buffer(200)
+    arr = (ctypes.c_void_p * 1)(ctypes.addressof(stale))
+    assert L.custen_compute_group(arr, 1, 0, None) == 2
+    assert b"not created by this library" in L.custen_last_error()
+    h = ctypes.create_string_buffer(200)
+    rc = L.custen_create_slab(h, cs.YP, cs.F64, 0, 3, 2, 64, 64, 32, 8, 1, 1, 1, 1, 1, 1, 0, 0, 5, 2, 2, 5, None)
+    assert rc == 2 and b"index must lie" in L.custen_last_error()
+    rc = L.custen_create_slab(h, cs.YP, cs.F64, 0, 1, 2, 64, 64, 32, 8, 1, 1, None, 1, 1, 1, 0, 0, 5, 2, 2, 5, None)
+    assert rc == 2 and b"halo_top is NULL" in L.custen_last_error()
