@@ -940,6 +940,9 @@ int custen_compute_group(cuSten_t* const* handles, int count, int offload, void*
         if (!priv_of(handles[k])) return fail_arg("custen_compute_group: handle %d was not created by this library", k);
         for (int j = 0; j < k; ++j)
             if (handles[j] == handles[k]) return fail_arg("custen_compute_group: handle %d appears twice", k);
+        if (handles[k]->deviceNum != handles[0]->deviceNum)
+            return fail_arg("custen_compute_group: handle %d is on device %d, handle 0 on device %d", k,
+                            handles[k]->deviceNum, handles[0]->deviceNum);
     }
     if (count == 0) return ST_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -96,8 +96,8 @@ int custen_compute_on_stream(cuSten_t* h, int offload, void* stream); /* same, a
 /* One Compute of each of `count` distinct handles, free to run at the same time: each handle's work runs
  * on its own first stream, after the work already queued on `stream` and before any work queued on
  * `stream` later. Use it for independent operators (e.g. several derivatives of one field into separate
- * outputs): on small fields one launch's tail then overlaps the next launch. Handles that write a buffer
- * another member reads must not be grouped. The reference computes one handle per call
+ * outputs): on small fields one launch's tail then overlaps the next launch. All handles and `stream`
+ * belong to one device. Handles that write a buffer another member reads must not be grouped. The reference computes one handle per call
  * (stencil_kernels.h:52-183); this has no counterpart there. */
 int custen_compute_group(cuSten_t* const* handles, int count, int offload, void* stream);
 int custen_swap(cuSten_t* h, void* dataInput);                      /* cuStenSwap2D*(h, dataInput) */
