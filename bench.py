@@ -218,26 +218,33 @@ def reference_gpu(args) -> dict:
     f = (torch.sin(3 * x)[None, :] * torch.cos(5 * x)[:, None] +
          (torch.rand((n, n), device=dev, dtype=torch.float64, generator=g) * 2e-3 - 1e-3)).contiguous()
     o = torch.zeros_like(f)
-    per, total = {}, 0.0
+    per, best_block, total = {}, {}, 0.0
     for (nm, v, H, L, R, V, T, B, w, fun, _) in operators(n):
         wt = torch.tensor(w, dtype=torch.float64, device=dev)
         d = 0 if v < 4 else (1 if v < 8 else 2)
         num_sten = H * V if d == 2 else (H if d == 0 else V)
         func = oracle.reference_fun_ptr(fun) if fun >= 0 else 0
+        best = None
+        for bx, by in ((32, 8), (32, 16), (32, 32)):   # the reference's BLOCK_X x BLOCK_Y, best of three
 
-        def call():
-            oracle.reference_compute(v, n, n, 1, 32, 8, o.data_ptr(), f.data_ptr(), wt.data_ptr(), num_sten=num_sten,
-                                     H=H, L=L, R=R, V=V, T=T, B=B, num_coe=len(w), func=func)
-        call()
-        reps = 3
-        t0 = time.perf_counter()
-        for _ in range(reps):
+            def call():
+                oracle.reference_compute(v, n, n, 1, bx, by, o.data_ptr(), f.data_ptr(), wt.data_ptr(),
+                                         num_sten=num_sten, H=H, L=L, R=R, V=V, T=T, B=B, num_coe=len(w), func=func)
             call()
-        dt = (time.perf_counter() - t0) / reps
-        total += dt
-        per[nm] = round(n * n / dt / 1e9, 3)
+            reps = 3
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                call()
+            dt = (time.perf_counter() - t0) / reps
+            if best is None or dt < best[0]:
+                best = (dt, f"{bx}x{by}")
+        total += best[0]
+        per[nm] = round(n * n / best[0] / 1e9, 3)
+        best_block[nm] = best[1]
     out["stencil_sweep"] = {"gpts_s": round(12 * n * n / total / 1e9, 3), "unit": "Gpts/s", "per_op": per,
-                            "config": f"{n}^2, the 12 operators of the headline sweep, BLOCK 32x8, numTiles 1",
+                            "block_per_op": best_block,
+                            "config": f"{n}^2, the 12 operators of the headline sweep, numTiles 1, each operator at "
+                                      f"its best BLOCK_X x BLOCK_Y of 32x8, 32x16, 32x32",
                             "method": "reference kernels, one launch per Compute, wall time of each synchronised "
                                       "Compute (XpFun with the shared-memory layout its kernel indexes)"}
     # WENO advection
