@@ -838,26 +838,34 @@ def run_size_sweep(cs, torch, dev, local, sizes=(1024, 2048, 4096, 8192), tiles=
             ms = sorted(times)[len(times) // 2]
             out[f"{n}_tiles{nt}"] = {"gpts_s": round(len(ops) * n * n / (ms * 1e-3) / 1e9, 3),
                                      "ms_per_sweep": round(ms, 4), "timing": "graph replay" if graph else "events"}
-            if graph is not None and group:
+            if group:
                 # the twelve operators are independent (one input, twelve outputs): one custen_compute_group
                 # call runs each on its handle's own stream, so that one launch's tail overlaps the next
-                g2 = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(g2, capture_error_mode="relaxed"):
-                    cs.compute_group(hs, cs.DEVICE, torch.cuda.current_stream(dev))
-                g2.replay()
+                g2 = None
+                if graph is not None:
+                    g2 = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g2, capture_error_mode="relaxed"):
+                        cs.compute_group(hs, cs.DEVICE, torch.cuda.current_stream(dev))
+                    g2.replay()
+                else:
+                    cs.compute_group(hs, cs.DEVICE, s)
                 torch.cuda.synchronize(dev)
                 times = []
                 for _ in range(reps):
                     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     e0.record(s)
-                    g2.replay()
+                    if g2 is not None:
+                        g2.replay()
+                    else:
+                        cs.compute_group(hs, cs.DEVICE, s)
                     e1.record(s)
                     torch.cuda.synchronize(dev)
                     times.append(e0.elapsed_time(e1))
                 ms2 = sorted(times)[len(times) // 2]
                 out[f"{n}_tiles{nt}"]["group"] = {
                     "gpts_s": round(len(ops) * n * n / (ms2 * 1e-3) / 1e9, 3), "ms_per_sweep": round(ms2, 4),
-                    "timing": "graph replay of one custen_compute_group call over the 12 handles"}
+                    "timing": ("graph replay of " if g2 is not None else "events around ") +
+                              "one custen_compute_group call over the 12 handles"}
                 del g2
             for h in hs:
                 h.destroy()
