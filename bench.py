@@ -542,6 +542,10 @@ def run_gpu(args, world, rank, local):
         ms32, per32, _ = timed_sweep(hs32, max(1, args.steps), 3)
         fp32 = {"gpts_s": round(pts_step / (ms32 / max(1, args.steps) * 1e-3) / 1e9, 3),
                 "hbm_gbs": round(8.0 * pts_step / (sum(per32) * 1e-3) / 1e9, 1), "per_op": {}}
+        g32, _ = timed_group(hs32, max(1, args.steps), 3)
+        fp32["group"] = {"gpts_s": round(pts_step / (g32 / max(1, args.steps) * 1e-3) / 1e9, 3),
+                         "gbs": round(8.0 * pts_step / (g32 / max(1, args.steps) * 1e-3) / 1e9, 1),
+                         "note": "the same sweep as one custen_compute_group call per step"}
         for (nm, *_r), ms, o32, o64, h32 in zip(ops, per32, outs32, outs64, hs32):
             d = o32.double() - o64
             fp32["per_op"][nm] = {
