@@ -50,11 +50,12 @@ struct ChConfig {
     int y_chunk;
     int pipe;
     int x_chunk;     // columns per chunk of the register-table x sweep (pipe 2, 3): 8 or 16
-    int rhs_split;   // 1: the right-hand side in two passes through GridDev::hbuf (batches only)
+    int rhs_split;   // 1: the right-hand side in two passes through GridDev::hbuf (batches only); 2: the same
+                     // with pass 2 pipelined (cp.async double buffer)
 };
 constexpr ChConfig kChDefault{4, 8, 3, 16, 0};   // configuration 12; needs no h buffer (server, one-grid step)
 constexpr int kChBatchDefault = 17;             // batches (they allocate the h buffer): two-pass right-hand side
-constexpr int kChConfigs = 19;
+constexpr int kChConfigs = 21;
 constexpr int kChCounters = 4;   // work counters per step (zeroed before it)
 ChConfig ch_config(int index);   // 0 .. kChConfigs-1
 void config_name(const ChConfig& c, char* name, size_t len);

@@ -254,6 +254,101 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs2_kernel(const GridDev* __rest
     }
 }
 
+// cp.async helpers (8-byte copies into shared memory, grouped, waited on by group count)
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Pass 2, pipelined (configurations with rhs_split = 2): the same expressions as ch_rhs2_kernel<double>,
+// so the same results, with the next work item's h window and cCurr / cOld blocks copied into the other
+// half of a shared-memory double buffer (cp.async) while the current item computes. ch_rhs2_kernel waits
+// on its loads (long-scoreboard stalls about 22 warps per issue at 32 grids of 512^2, FP64 pipe 68% busy);
+// here they are in flight during the previous item's arithmetic. The buffer is dynamic shared memory:
+// kRhs2PipeWords doubles per half.
+constexpr int kRhs2H = 34 * 35, kRhs2C = 32 * 33;
+constexpr int kRhs2PipeWords = kRhs2H + 2 * kRhs2C;
+constexpr size_t kRhs2PipeBytes = 2 * kRhs2PipeWords * sizeof(double);
+
+template <int NW>
+__device__ __forceinline__ void rhs2_issue(double* buf, const GridDev& gd, const Item& item, int parity, int tid) {
+    constexpr int NT = NW * BLK;
+    const int n = gd.n;
+    const double* cur = parity ? gd.buf[1] : gd.buf[0];
+    const double* old = parity ? gd.buf[0] : gd.buf[1];
+    const int bpr = n / BLK;
+    const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
+    double* hh = buf;
+    double* cu = buf + kRhs2H;
+    double* ol = cu + kRhs2C;
+    for (int e = tid; e < 34 * 34; e += NT) {
+        const int r = e / 34, c = e - r * 34;
+        int gy = y0 - 1 + r, gx = x0 - 1 + c;
+        gy = gy < 0 ? gy + n : (gy >= n ? gy - n : gy);
+        gx = gx < 0 ? gx + n : (gx >= n ? gx - n : gx);
+        cp_async8(hh + r * 35 + c, gd.hbuf + (size_t)gy * n + gx);
+    }
+    for (int e = tid; e < 32 * 32; e += NT) {
+        const int r = e >> 5, c = e & 31;
+        const size_t q = (size_t)(y0 + r) * n + x0 + c;
+        cp_async8(cu + r * 33 + c, cur + q);
+        cp_async8(ol + r * 33 + c, old + q);
+    }
+}
+
+template <int NW>
+__global__ void __launch_bounds__(NW * BLK) ch_rhs2_pipe_kernel(const GridDev* __restrict__ grids,
+                                                                const Item* __restrict__ items, int n_items,
+                                                                int parity, unsigned int* counter) {
+    extern __shared__ __align__(16) double rhs2_smem[];
+    __shared__ int s_next[2];
+    const int tid = threadIdx.x;
+    const int lane = tid & (BLK - 1), warp = tid / BLK;
+    const volatile double* factors = g_rhs_factors;
+    const double m_four = factors[1], m_two_thirds = factors[2];
+    if (tid == 0) s_next[1] = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    int it_cur = s_next[1];
+    if (it_cur < n_items) rhs2_issue<NW>(rhs2_smem, grids[items[it_cur].grid], items[it_cur], parity, tid);
+    cp_async_commit();
+    for (int k = 0;; ++k) {
+        if (it_cur >= n_items) break;   // uniform: every thread read the same claim
+        if (tid == 0) s_next[k & 1] = (int)atomicAdd(counter, 1u);
+        __syncthreads();   // the claim is visible; every thread is done with the other half of the buffer
+        const int it_next = s_next[k & 1];
+        if (it_next < n_items)
+            rhs2_issue<NW>(rhs2_smem + ((k + 1) & 1) * kRhs2PipeWords, grids[items[it_next].grid], items[it_next],
+                           parity, tid);
+        cp_async_commit();
+        cp_async_wait<1>();   // this thread's copies of the current item have landed
+        __syncthreads();      // and every other thread's
+        const double* hh = rhs2_smem + (k & 1) * kRhs2PipeWords;
+        const double* cu = hh + kRhs2H;
+        const double* ol = cu + kRhs2C;
+        const Item item = items[it_cur];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n;
+        const int bpr = n / BLK;
+        const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
+        const int j = lane;
+        double* out = gd.tmp + (size_t)y0 * n + x0 + j;
+#pragma unroll 4
+        for (int rr = warp; rr < BLK; rr += NW) {
+            const double lap = fma(m_four, hh[(rr + 1) * 35 + j + 1],
+                                   (hh[rr * 35 + j + 1] + hh[(rr + 2) * 35 + j + 1]) +
+                                       (hh[(rr + 1) * 35 + j] + hh[(rr + 1) * 35 + j + 2]));
+            const double dco = cu[rr * 33 + j] - ol[rr * 33 + j];
+            if (!in_bounds((long long)(y0 + rr) * n + x0 + j, 0, (long long)n * n)) continue;
+            out[(size_t)rr * n] = fma(m_two_thirds, dco, lap);
+        }
+        it_cur = it_next;
+    }
+    cp_async_wait<0>();
+}
+
 // ------------------------------------------------------------------------------------------------
 // K2: x sweep (lane = row), 32-column chunks through shared memory
 // ------------------------------------------------------------------------------------------------
@@ -526,13 +621,6 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
 // per SM. Here the loads of the next chunk are in flight during the current chain, they occupy no
 // registers, and the table entries of the next chunk are read one chunk ahead. The arithmetic, its order
 // and so every result are those of the kernels above.
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // x sweep (lane = row) over XC-column chunks. Each lane copies, and later writes back, the elements
 // e = lane + 32 j of a chunk (row e / XC, column e % XC): one row segment (XC = 32) or two (XC = 16) per
@@ -1139,13 +1227,14 @@ ChConfig ch_config(int index) {
         {1, 32, 0, 16}, {2, 32, 0, 16}, {4, 32, 0, 16}, {1, 16, 0, 16}, {2, 16, 0, 16}, {4, 16, 0, 16},
         {2, 16, 1, 16}, {4, 16, 1, 16}, {2, 32, 1, 16}, {4, 32, 1, 16}, {4, 16, 2, 16}, {4, 32, 2, 16},
         {4, 8, 3, 16},  {4, 16, 3, 16}, {4, 8, 3, 8},   {4, 4, 3, 8},   {4, 4, 3, 16},
-        {4, 8, 3, 16, 1}, {2, 8, 3, 16, 1}};
+        {4, 8, 3, 16, 1}, {2, 8, 3, 16, 1}, {4, 8, 3, 16, 2}, {2, 8, 3, 16, 2}};
     return tab[(index >= 0 && index < kChConfigs) ? index : 0];
 }
 
 void config_name(const ChConfig& c, char* name, size_t len) {
     if (c.pipe >= 2)
-        snprintf(name, len, "rhs_warps%d%s_ychunk%d_pipe_regtab%s_xchunk%d", c.rhs_warps, c.rhs_split ? "_2pass" : "",
+        snprintf(name, len, "rhs_warps%d%s_ychunk%d_pipe_regtab%s_xchunk%d", c.rhs_warps,
+                 c.rhs_split == 2 ? "_2pass_pipe" : (c.rhs_split ? "_2pass" : ""),
                  c.y_chunk, c.pipe == 3 ? "_xy" : "", c.x_chunk);
     else
         snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
@@ -1154,9 +1243,36 @@ void config_name(const ChConfig& c, char* name, size_t len) {
 // The two passes of the split right-hand side; pass 2 claims work through the step's fourth counter.
 // Pass 2 runs in FP64 in both variants: the precision variant's h buffer holds FP32 values, whose FP64
 // Laplacian is exact, so its mass is conserved to FP64 rounding (the one-pass kernel does the same).
+// Pass 2 pipelined: dynamic shared memory beyond 48 KB, allowed once per device and kernel.
+template <int NW>
+static cudaError_t launch_rhs2_pipe(int grid, const GridDev* g, const Item* it, int n, int parity, unsigned int* ctr,
+                                    cudaStream_t s) {
+    static std::atomic<int> ready[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!ready[dev].load(std::memory_order_acquire)) {
+        cudaError_t e = cudaFuncSetAttribute(ch_rhs2_pipe_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kRhs2PipeBytes);
+        if (e != cudaSuccess) return e;
+        ready[dev].store(1, std::memory_order_release);
+    }
+    ch_rhs2_pipe_kernel<NW><<<grid, NW * BLK, kRhs2PipeBytes, s>>>(g, it, n, parity, ctr);
+    return cudaGetLastError();
+}
+
 template <typename T>
-static void launch_rhs2(int nw, int grid, const GridDev* g, const Item* it, int n, int parity, unsigned int* ctr,
-                        cudaStream_t s) {
+static cudaError_t launch_rhs2(int nw, int grid, const GridDev* g, const Item* it, int n, int parity,
+                               unsigned int* ctr, cudaStream_t s, bool pipe, int sms) {
+    if (pipe) {   // four CTAs per SM fit the double buffer
+        const int gp = std::max(1, std::min(n, sms * 4));
+        if (nw == 4) {
+            ch_h_kernel<T, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr);
+            return launch_rhs2_pipe<4>(gp, g, it, n, parity, ctr + 3, s);
+        }
+        ch_h_kernel<T, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr);
+        return launch_rhs2_pipe<2>(gp, g, it, n, parity, ctr + 3, s);
+    }
     if (nw == 4) {
         ch_h_kernel<T, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr);
         ch_rhs2_kernel<double, 4><<<grid, 4 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
@@ -1164,6 +1280,7 @@ static void launch_rhs2(int nw, int grid, const GridDev* g, const Item* it, int 
         ch_h_kernel<T, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr);
         ch_rhs2_kernel<double, 2><<<grid, 2 * BLK, 0, s>>>(g, it, n, parity, ctr + 3);
     }
+    return cudaGetLastError();
 }
 
 template <typename T>
@@ -1183,8 +1300,12 @@ cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grid
     const int g1 = std::max(1, std::min(n_rhs, sms * 32 / c.rhs_warps));
     const int g23 = std::max(1, std::min(n_rows, sms * 16));
     if (c.rhs_split) {
-        if (rhs_fp32) launch_rhs2<float>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
-        else launch_rhs2<double>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
+        const cudaError_t e2 =
+            rhs_fp32 ? launch_rhs2<float>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s,
+                                          c.rhs_split == 2, sms)
+                     : launch_rhs2<double>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s,
+                                           c.rhs_split == 2, sms);
+        if (e2 != cudaSuccess) return e2;
     } else if (rhs_fp32) {
         launch_rhs<float>(c.rhs_warps, g1, grids, items_rhs, n_rhs, parity, counters, s);
     } else {
@@ -1596,7 +1717,7 @@ int custen_ch_batch_step(void* h, int steps, int use_graph) {
     if (!b || steps < 0) return ch_fail_arg("invalid arguments");
     cudaSetDevice(b->device);
     int left = steps;
-    const int per_step = 3 + batch_config(b).rhs_split;   // kernel launches in one step
+    const int per_step = 3 + (batch_config(b).rhs_split ? 1 : 0);   // kernel launches in one step
     if (use_graph && left >= 2) {
         int st = capture_pairs(b);
         if (st) return st;
