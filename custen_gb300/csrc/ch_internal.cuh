@@ -54,7 +54,8 @@ struct ChConfig {
                      // with pass 2 pipelined (cp.async double buffer)
 };
 constexpr ChConfig kChDefault{4, 8, 3, 16, 0};   // configuration 12; needs no h buffer (server, one-grid step)
-constexpr int kChBatchDefault = 17;             // batches (they allocate the h buffer): two-pass right-hand side
+constexpr int kChBatchDefault = 20;             // batches (they allocate the h buffer): two-pass right-hand side,
+                                                // pass 2 pipelined, 8 warps per CTA
 constexpr int kChConfigs = 21;
 constexpr int kChCounters = 4;   // work counters per step (zeroed before it)
 ChConfig ch_config(int index);   // 0 .. kChConfigs-1
