@@ -41,7 +41,6 @@
 #include "../../include/custen_gb300.h"
 #include "ch_internal.cuh"
 #include "checked.cuh"
-#include "cvt_int.cuh"
 
 namespace custen {
 namespace ch {
@@ -69,14 +68,6 @@ namespace ch {
 // (507 against 602-628 G FMA/s measured) than one whose operands are all registers. The values, and
 // so the results, are the same as with literals.
 __device__ double g_rhs_factors[3] = {2.0, -4.0, -2.0 / 3.0};
-
-// Conversions of the precision variant (T = float) on the integer pipes (cvt_int.cuh): the same values as
-// the hardware conversions, which on GB300 would occupy the FP64 pipe. Identity for T = double.
-template <typename T> __device__ __forceinline__ T to_t(double x);
-template <> __device__ __forceinline__ double to_t<double>(double x) { return x; }
-template <> __device__ __forceinline__ float to_t<float>(double x) { return f64_to_f32_rn(x); }
-__device__ __forceinline__ double to_d(double x) { return x; }
-__device__ __forceinline__ double to_d(float x) { return f32_to_f64(x); }
 
 template <typename T, int NW>
 __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restrict__ grids,
@@ -109,8 +100,8 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
         const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
         // sigma_lin and sigma_nl, exactly: the far weight of the biharmonic is -sigma_lin, the north weight
         // of the Laplacian sigma_nl (the table stores the weights as pattern * sigma)
-        const T s_lin = to_t<T>(-tab[7 * m + 8 + 2]);
-        const T s_nl = to_t<T>(tab[7 * m + 33 + 1]);
+        const T s_lin = (T)(-tab[7 * m + 8 + 2]);
+        const T s_nl = (T)tab[7 * m + 33 + 1];
         // stage the 36 x 36 window (periodic wrap)
 #pragma unroll 4
         for (int e = tid; e < 36 * 36; e += NT) {
@@ -120,7 +111,7 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
             gx = gx < 0 ? gx + n : (gx >= n ? gx - n : gx);
             const double cv = cur[(size_t)gy * n + gx];
             const double ov = old[(size_t)gy * n + gx];
-            const T c32 = to_t<T>(cv), o32 = to_t<T>(ov);
+            const T c32 = (T)cv, o32 = (T)ov;
             cb[r][c] = fma(two, c32, -o32);
             if (r >= 1 && r < 35 && c >= 1 && c < 35) hh[r - 1][c - 1] = s_nl * fma(c32 * c32, c32, -c32);
             if (r >= 2 && r < 34 && c >= 2 && c < 34) dco[r - 2][c - 2] = cv - ov;
@@ -142,9 +133,9 @@ __global__ void __launch_bounds__(NW * BLK) ch_rhs_kernel(const GridDev* __restr
         double* out = gd.tmp + (size_t)y0 * n + x0 + j;
 #pragma unroll 4
         for (int rr = warp; rr < BLK; rr += NW) {
-            const double lap = fma(m_four_d, to_d(hh[rr + 1][j + 1]),
-                                   (to_d(hh[rr][j + 1]) + to_d(hh[rr + 2][j + 1])) +
-                                       (to_d(hh[rr + 1][j]) + to_d(hh[rr + 1][j + 2])));
+            const double lap = fma(m_four_d, (double)hh[rr + 1][j + 1],
+                                   ((double)hh[rr][j + 1] + (double)hh[rr + 2][j + 1]) +
+                                       ((double)hh[rr + 1][j] + (double)hh[rr + 1][j + 2]));
             if (!in_bounds((long long)(y0 + rr) * n + x0 + j, 0, (long long)n * n)) continue;
             out[(size_t)rr * n] = fma(m_two_thirds_d, dco[rr][j], lap);
         }
@@ -185,8 +176,8 @@ __global__ void __launch_bounds__(NW * BLK) ch_h_kernel(const GridDev* __restric
         const double* tab = gd.tab;
         const int bpr = n / BLK;
         const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
-        const T s_lin = to_t<T>(-tab[7 * m + 8 + 2]);
-        const T s_nl = to_t<T>(tab[7 * m + 33 + 1]);
+        const T s_lin = (T)(-tab[7 * m + 8 + 2]);
+        const T s_nl = (T)tab[7 * m + 33 + 1];
 #pragma unroll 4
         for (int e = tid; e < 34 * 34; e += NT) {
             const int r = e / 34, c = e - r * 34;
@@ -195,7 +186,7 @@ __global__ void __launch_bounds__(NW * BLK) ch_h_kernel(const GridDev* __restric
             gx = gx < 0 ? gx + n : (gx >= n ? gx - n : gx);
             const double cv = cur[(size_t)gy * n + gx];
             const double ov = old[(size_t)gy * n + gx];
-            const T c32 = to_t<T>(cv), o32 = to_t<T>(ov);
+            const T c32 = (T)cv, o32 = (T)ov;
             cb[r][c] = fma(two, c32, -o32);
             if (r >= 1 && r < 33 && c >= 1 && c < 33) gg[r - 1][c - 1] = s_nl * fma(c32 * c32, c32, -c32);
         }
@@ -205,7 +196,7 @@ __global__ void __launch_bounds__(NW * BLK) ch_h_kernel(const GridDev* __restric
             const int r = e / 32, c = e - r * 32;
             const T lap = fma(m_four, cb[r + 1][c + 1], (cb[r][c + 1] + cb[r + 2][c + 1]) + (cb[r + 1][c] + cb[r + 1][c + 2]));
             const long long q = (long long)(y0 + r) * n + x0 + c;
-            if (in_bounds(q, 0, (long long)n * n)) gd.hbuf[q] = to_d(fma(-s_lin, lap, gg[r][c]));
+            if (in_bounds(q, 0, (long long)n * n)) gd.hbuf[q] = (double)fma(-s_lin, lap, gg[r][c]);
         }
         __syncthreads();
     }

@@ -190,10 +190,6 @@ int custen_device_error(unsigned int* flags, int clear);
  * raised and the kernel returns. *flags receives the flags afterwards (left set). No copy fails and
  * nothing traps; the context stays usable. */
 int custen_selftest_wait_expiry(long long rounds, unsigned int* flags);
-/* Checks the library's integer-pipe FP64 <-> FP32 conversions (used by the FP32-stencil Cahn-Hilliard
- * variant) against the hardware conversions on n seeded values of each kind; *mismatches counts the
- * results whose encodings differ (0 expected). No reference counterpart. */
-int custen_selftest_conversions(unsigned long long n, unsigned long long seed, unsigned long long* mismatches);
 
 /* ---- batched pentadiagonal systems (cuPentBatch, cuPentCahnADI/src/cuPentBatch.cu) ----
  * Interleaved layout: element (row i, system s) of each diagonal and of b at [i * batch + s]; ds, dl
