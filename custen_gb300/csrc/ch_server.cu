@@ -2,7 +2,7 @@
 //
 // Requests (grid size n, step count, initial field, arrival time) arrive over time. The loop admits
 // arrived requests first-come first-served while their device memory fits the HBM budget: their two
-// field buffers, work field and row ends are allocated stream-ordered (cudaMallocAsync, no device
+// field buffers, work field, h field and row ends are allocated stream-ordered (cudaMallocAsync, no device
 // synchronisation) and their pre-factored solver table is shared by every resident grid of the same
 // size. All resident grids then advance together, a chunk of steps at a time, through the same
 // persistent kernels as the batch solver (ch_solver.cu): one launch per kernel covers every grid.
@@ -122,7 +122,8 @@ static int srv_arg(const std::string& m) {
         if (_e != cudaSuccess) return srv_fail(_e, what); \
     } while (0)
 
-static size_t grid_bytes(int n) { return 3 * (size_t)n * n * sizeof(double) + 2 * (size_t)n * sizeof(double); }
+// per grid: cCurr, cOld, the work field and the h field of the two-pass right-hand side, plus 2 n row ends
+static size_t grid_bytes(int n) { return 4 * (size_t)n * n * sizeof(double) + 2 * (size_t)n * sizeof(double); }
 
 static int grow(void** p, size_t* cap, size_t need, size_t elem, cudaStream_t s) {
     if (need <= *cap) return 0;
@@ -199,9 +200,9 @@ static int admit(Server* S, int id, double now) {
         }
     }
     const size_t f = (size_t)r.n * r.n * sizeof(double);
-    double* p[4] = {nullptr, nullptr, nullptr, nullptr};
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
-        step(alloc(&p[k], k < 3 ? f : 2 * (size_t)r.n * sizeof(double)), "Allocating a grid");
+    double* p[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // cCurr, cOld, tmp, row ends, h
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+        step(alloc(&p[k], k == 3 ? 2 * (size_t)r.n * sizeof(double) : f), "Allocating a grid");
     double m = 0.0;
     if (e == cudaSuccess) {
         if (!r.c0.empty()) {
@@ -244,6 +245,7 @@ static int admit(Server* S, int id, double now) {
     r.g.buf[S->parity ^ 1] = p[1];    // cOld
     r.g.tmp = p[2];
     r.g.ends = p[3];
+    r.g.hbuf = p[4];
     r.g.tab = t.ptr;
     r.g.n = r.n;
     r.mean0 = m / ((double)r.n * r.n);
@@ -271,7 +273,7 @@ static int retire(Server* S, int id, double now_after) {
     SRV_TRY(cudaStreamSynchronize(S->stream), "Retiring");
     r.mean_end = m / ((double)r.n * r.n);
     r.done_t = now_after;
-    for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends}) SRV_TRY(cudaFreeAsync(p, S->stream), "Freeing a grid");
+    for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends, r.g.hbuf}) SRV_TRY(cudaFreeAsync(p, S->stream), "Freeing a grid");
     S->used -= (double)r.bytes;
     TableRef& t = S->tables[r.table_key];
     if (--t.refs == 0) {
@@ -317,7 +319,7 @@ static bool write_snapshot(Server* S, Request& r, std::string* err) {
 // Take a resident request out of the run as failed: release its memory, record why.
 static int drop(Server* S, int id, const std::string& why, double now) {
     Request& r = S->reqs[id];
-    for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends}) SRV_TRY(cudaFreeAsync(p, S->stream), "Freeing a grid");
+    for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends, r.g.hbuf}) SRV_TRY(cudaFreeAsync(p, S->stream), "Freeing a grid");
     S->used -= (double)r.bytes;
     TableRef& t = S->tables[r.table_key];
     if (--t.refs == 0) {
@@ -335,10 +337,10 @@ static int drop(Server* S, int id, const std::string& why, double now) {
 static int enqueue_steps(Server* S, int k) {
     for (int s = 0; s < k; ++s) {
         SRV_TRY(cudaMemsetAsync(S->counters, 0, kChCounters * sizeof(unsigned int), S->stream), "Resetting counters");
-        SRV_TRY(launch_ch_step(kChDefault, S->rhs_fp32 != 0, S->grids_d, S->items_rhs_d, S->n_rhs, S->items_rows_d,
-                               S->n_rows, S->parity, S->counters, S->sms, S->stream),
+        SRV_TRY(launch_ch_step(ch_config(kChBatchDefault), S->rhs_fp32 != 0, S->grids_d, S->items_rhs_d, S->n_rhs,
+                               S->items_rows_d, S->n_rows, S->parity, S->counters, S->sms, S->stream),
                 "Launching a step");
-        S->launches += 3;
+        S->launches += 4;
         S->parity ^= 1;
     }
     return 0;
@@ -623,7 +625,7 @@ int custen_ch_server_destroy(void* h) {
     cudaStreamSynchronize(S->stream);
     for (int id : S->active) {
         Request& r = S->reqs[id];
-        for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends}) cudaFreeAsync(p, S->stream);
+        for (double* p : {r.g.buf[0], r.g.buf[1], r.g.tmp, r.g.ends, r.g.hbuf}) cudaFreeAsync(p, S->stream);
     }
     for (auto& t : S->tables)
         if (t.second.ptr) cudaFreeAsync(t.second.ptr, S->stream);

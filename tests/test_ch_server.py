@@ -60,7 +60,7 @@ def test_served_2048_request_in_mix_equals_alone(gpu):
 
 def test_budget_limits_resident_set(gpu):
     """A budget that holds two 128^2 grids at a time: four requests still all complete."""
-    per_grid = 3 * 128 * 128 * 8 + 2 * 128 * 8
+    per_grid = 4 * 128 * 128 * 8 + 2 * 128 * 8
     table = (7 * 126 + 42) * 8
     srv = cs.CahnHilliardServer(hbm_budget_bytes=2 * per_grid + table + 1024, chunk_steps=3, keep_results=False)
     for k in range(4):
