@@ -1299,7 +1299,7 @@ def main():
     ap.add_argument("--skip-pent", action="store_true")
     ap.add_argument("--pent-batch", type=int, default=1 << 18, help="systems in the pentadiagonal leg (256 unknowns each)")
     ap.add_argument("--ch-config", type=int, default=-1,
-                    help="pin the CH batch kernel configuration (0..20) instead of tuning it")
+                    help="pin the CH batch kernel configuration (0..21) instead of tuning it")
     ap.add_argument("--stage-chunk-mb", type=int, default=0,
                     help="chunk size of the host-memory staging path (0: the library default)")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],

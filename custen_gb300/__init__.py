@@ -480,7 +480,7 @@ class CahnHilliardBatch:
         return buf.value.decode()
 
     def set_config(self, index: int) -> None:
-        """Pin the kernel configuration (0 .. 20; -1: the default)."""
+        """Pin the kernel configuration (0 .. 21; -1: the default)."""
         _ch_check(lib().custen_ch_batch_set_config(self.h, int(index)))
 
     def save(self, sim: int, path, time: float = 0.0) -> None:

@@ -52,13 +52,17 @@ struct ChConfig {
     int x_chunk;     // columns per chunk of the register-table x sweep (pipe 2, 3): 8 or 16
     int rhs_split;   // 1: the right-hand side in two passes through GridDev::hbuf (batches only); 2: the same
                      // with pass 2 pipelined (cp.async double buffer)
+    int ysplit;      // 1: the y sweep's correction and update as element-wise kernels around the recurrences
+                     // (pipe 3 only; for batches with few lines per SM)
 };
 constexpr ChConfig kChDefault{4, 8, 3, 16, 0};   // configuration 12; needs no h buffer (server, one-grid step)
 constexpr int kChBatchDefault = 20;             // batches (they allocate the h buffer): two-pass right-hand side,
                                                 // pass 2 pipelined, 8 warps per CTA
-constexpr int kChConfigs = 21;
+constexpr int kChConfigs = 22;
+constexpr int kChSplitConfig = 21;             // configuration 20 with the split y sweep
 constexpr int kChCounters = 4;   // work counters per step (zeroed before it)
 ChConfig ch_config(int index);   // 0 .. kChConfigs-1
+int ch_launches_per_step(const ChConfig& c);
 void config_name(const ChConfig& c, char* name, size_t len);
 
 // One step of every grid of a work list: right-hand side (one or two passes), x sweep, y sweep (3 or 4

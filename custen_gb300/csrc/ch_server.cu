@@ -337,10 +337,14 @@ static int drop(Server* S, int id, const std::string& why, double now) {
 static int enqueue_steps(Server* S, int k) {
     for (int s = 0; s < k; ++s) {
         SRV_TRY(cudaMemsetAsync(S->counters, 0, kChCounters * sizeof(unsigned int), S->stream), "Resetting counters");
-        SRV_TRY(launch_ch_step(ch_config(kChBatchDefault), S->rhs_fp32 != 0, S->grids_d, S->items_rhs_d, S->n_rhs,
-                               S->items_rows_d, S->n_rows, S->parity, S->counters, S->sms, S->stream),
+        // Fewer 32-line warps than FP64 sub-partitions (4 per SM): the sweeps are bound by a warp's own FP64
+        // instruction count, so the y sweep's correction and update run as element-wise kernels. Every
+        // configuration computes the same values, so a request's result does not depend on the choice.
+        const ChConfig cfg = ch_config(S->n_rows < 4 * S->sms ? kChSplitConfig : kChBatchDefault);
+        SRV_TRY(launch_ch_step(cfg, S->rhs_fp32 != 0, S->grids_d, S->items_rhs_d, S->n_rhs, S->items_rows_d,
+                               S->n_rows, S->parity, S->counters, S->sms, S->stream),
                 "Launching a step");
-        S->launches += 4;
+        S->launches += ch_launches_per_step(cfg);
         S->parity ^= 1;
     }
     return 0;

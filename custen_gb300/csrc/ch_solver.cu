@@ -1222,6 +1222,184 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_pipe_rt_kernel(const GridDev* _
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// K3 split in three (configurations with ysplit): for batches too small to fill the GPU with line warps.
+// ch_xcorr_kernel applies the x sweep's rank-2 correction to the work field, ch_ysolve_split_kernel runs
+// the y recurrences alone and leaves each column's two cyclic unknowns in GridDev::ends, and
+// ch_update_kernel forms cNew = cBar + delta. The expressions are those of ch_ysolve_pipe_rt_kernel, so
+// the results are the same bit for bit. A warp's FP64 instruction holds its sub-partition's FP64 pipe for
+// 64 cycles however few lanes it has, so a column's time in the y sweep is its warp's FP64 instruction
+// count: 5 per element here against 11 in the fused kernel, while the correction and the update spread
+// over every SM as element-wise kernels.
+// ------------------------------------------------------------------------------------------------
+// One 32 x 32 block of a grid per CTA (the right-hand side's work list): t[y][x] -= inv1[x] x2(y) +
+// inv2[x] x1(y) for the columns x < n - 2 of the block's rows, as fma(-inv1, x2, fma(-inv2, x1, t)).
+__global__ void __launch_bounds__(256) ch_xcorr_kernel(const GridDev* __restrict__ grids,
+                                                       const Item* __restrict__ items) {
+    const Item item = items[blockIdx.x];
+    const GridDev gd = grids[item.grid];
+    const int n = gd.n, m = n - 2;
+    const int bpr = n / BLK;
+    const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
+    const int x = x0 + (threadIdx.x & (BLK - 1));
+    if (x >= m) return;
+    const double cx1 = gd.tab[5 * m + x], cx2 = gd.tab[6 * m + x];
+    for (int r = threadIdx.x / BLK; r < BLK; r += blockDim.x / BLK) {
+        const int y = y0 + r;
+        const long long q = (long long)y * n + x;
+        if (!in_bounds(q, 0, (long long)n * n)) continue;
+        gd.tmp[q] = fma(-cx1, gd.ends[2 * y], fma(-cx2, gd.ends[2 * y + 1], gd.tmp[q]));
+    }
+}
+
+// One 32 x 32 block per CTA: cNew = cBar + delta written over cOld (cuPentCahnADI.cu:58-69, 89-100), delta
+// from the banded y solution in the work field and the column's cyclic unknowns in GridDev::ends.
+__global__ void __launch_bounds__(256) ch_update_kernel(const GridDev* __restrict__ grids,
+                                                        const Item* __restrict__ items, int parity) {
+    const Item item = items[blockIdx.x];
+    const GridDev gd = grids[item.grid];
+    const int n = gd.n, m = n - 2;
+    const int bpr = n / BLK;
+    const int y0 = (item.block / bpr) * BLK, x0 = (item.block % bpr) * BLK;
+    const int x = x0 + (threadIdx.x & (BLK - 1));
+    const double two = ((const volatile double*)g_rhs_factors)[0];
+    const double x2 = gd.ends[2 * x], x1 = gd.ends[2 * x + 1];
+    const double* cur = parity ? gd.buf[1] : gd.buf[0];
+    double* old = parity ? gd.buf[0] : gd.buf[1];
+    for (int r = threadIdx.x / BLK; r < BLK; r += blockDim.x / BLK) {
+        const int y = y0 + r;
+        const long long q = (long long)y * n + x;
+        double dlt;
+        if (y < m) dlt = fma(-gd.tab[5 * m + y], x2, fma(-gd.tab[6 * m + y], x1, gd.tmp[q]));
+        else dlt = (y == m) ? x2 : x1;
+        const double cbar = fma(two, cur[q], -old[q]);
+        if (in_bounds(q, 0, (long long)n * n)) old[q] = cbar + dlt;
+    }
+}
+
+template <int CH>
+__global__ void __launch_bounds__(BLK) ch_ysolve_split_kernel(const GridDev* __restrict__ grids,
+                                                             const Item* __restrict__ items, int n_items, int parity,
+                                                             unsigned int* counter) {
+    __shared__ double vb[2][CH][BLK];
+    __shared__ int s_item;
+    const int lane = threadIdx.x;
+    for (;;) {
+        if (lane == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncwarp();
+        const int it = s_item;
+        __syncwarp();
+        if (it >= n_items) break;
+        const Item item = items[it];
+        const GridDev gd = grids[item.grid];
+        const int n = gd.n, m = n - 2;
+        const double* tab = gd.tab;
+        const double* ds = tab;
+        const double* dl = tab + m;
+        const double* rd = tab + 2 * m;
+        const double* du = tab + 3 * m;
+        const double* dw = tab + 4 * m;
+        const int x = item.block * BLK + lane;
+        double* t = gd.tmp;
+        const int nb = n / CH;
+        auto issue = [&](int bb, int b, bool below_m) {
+            const int yb = bb * CH;
+            const double* src = t + (size_t)yb * n + x;
+#pragma unroll 4
+            for (int k = 0; k < CH; ++k, src += n)
+                if (!below_m || yb + k < m) cp_async8(&vb[b][k][lane], src);
+            cp_async_commit();
+        };
+        // forward elimination along y
+        double b1 = 0.0, b2 = 0.0, r2 = 0.0, r1 = 0.0;
+        issue(0, 0, false);
+        for (int bb = 0; bb < nb; ++bb) {
+            const int b = bb & 1, yb = bb * CH;
+            double ts[CH], tl[CH], tr[CH];
+#pragma unroll
+            for (int k = 0; k < CH; ++k) {
+                const bool in = yb + k < m;
+                ts[k] = in ? __ldg(ds + yb + k) : 0.0;
+                tl[k] = in ? __ldg(dl + yb + k) : 0.0;
+                tr[k] = in ? __ldg(rd + yb + k) : 0.0;
+            }
+            if (bb + 1 < nb) {
+                issue(bb + 1, b ^ 1, false);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+#pragma unroll
+            for (int k = 0; k < CH; ++k) {
+                const int y = yb + k;
+                const double a_s = ts[k], a_l = tl[k];
+                const double a_r = tr[k];
+                const double vk = vb[b][k][lane];
+                const double val = vk;   // corrected by ch_xcorr_kernel
+                if (y < m) {
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
+                    b2 = b1;
+                    b1 = w;
+                    if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
+                } else if (y == m) {
+                    r2 = val;
+                } else {
+                    r1 = val;
+                }
+            }
+        }
+        // backward substitution (rows below m only; the lane re-reads what it stored above)
+        double f1 = 0.0, f2 = 0.0, y0v = 0.0, y1v = 0.0, ym2 = 0.0, ym1 = 0.0;
+        issue(nb - 1, 0, true);
+        for (int j = 0; j < nb; ++j) {
+            const int bb = nb - 1 - j, b = j & 1, yb = bb * CH;
+            double tu[CH], tw[CH];
+#pragma unroll
+            for (int k = 0; k < CH; ++k) {
+                const bool in = yb + k < m;
+                tu[k] = in ? __ldg(du + yb + k) : 0.0;
+                tw[k] = in ? __ldg(dw + yb + k) : 0.0;
+            }
+            if (bb > 0) {
+                issue(bb - 1, b ^ 1, true);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+#pragma unroll
+            for (int k = CH - 1; k >= 0; --k) {
+                const int y = yb + k;
+                const double a_u = tu[k], a_w = tw[k];
+                if (y < m) {
+                    double w = fma(-a_u, f1, vb[b][k][lane]);
+                    w = fma(-a_w, f2, w);
+                    f2 = f1;
+                    f1 = w;
+                    if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
+                    if (y == m - 1) ym1 = w;
+                    if (y == m - 2) ym2 = w;
+                    if (y == 1) y1v = w;
+                    if (y == 0) y0v = w;
+                }
+            }
+        }
+        const double* om = tab + 7 * m;
+        const double a = om[4], b = om[5], d = om[6], e = om[7];
+        const double nx2 = r2 - (e * y0v + a * ym2 + b * ym1);
+        const double nx1 = r1 - (d * y0v + e * y1v + a * ym1);
+        const double x2 = om[0] * nx2 + om[1] * nx1;
+        const double x1 = om[2] * nx2 + om[3] * nx1;
+        // the column's two cyclic unknowns, for ch_update_kernel (the x sweep's row ends were consumed
+        // by ch_xcorr_kernel, so their buffer is free)
+        gd.ends[2 * x] = x2;
+        gd.ends[2 * x + 1] = x1;
+    }
+}
+
+int ch_launches_per_step(const ChConfig& c) { return 3 + (c.rhs_split ? 1 : 0) + (c.ysplit ? 2 : 0); }
+
 ChConfig ch_config(int index) {
     // {warps per right-hand-side CTA, y-sweep rows per batch, sweep kind, x-sweep columns per chunk (kinds 2,
     // 3), two-pass right-hand side}
@@ -1229,15 +1407,15 @@ ChConfig ch_config(int index) {
         {1, 32, 0, 16}, {2, 32, 0, 16}, {4, 32, 0, 16}, {1, 16, 0, 16}, {2, 16, 0, 16}, {4, 16, 0, 16},
         {2, 16, 1, 16}, {4, 16, 1, 16}, {2, 32, 1, 16}, {4, 32, 1, 16}, {4, 16, 2, 16}, {4, 32, 2, 16},
         {4, 8, 3, 16},  {4, 16, 3, 16}, {4, 8, 3, 8},   {4, 4, 3, 8},   {4, 4, 3, 16},
-        {4, 8, 3, 16, 1}, {2, 8, 3, 16, 1}, {4, 8, 3, 16, 2}, {8, 8, 3, 16, 2}};
+        {4, 8, 3, 16, 1}, {2, 8, 3, 16, 1}, {4, 8, 3, 16, 2}, {8, 8, 3, 16, 2}, {8, 8, 3, 16, 2, 1}};
     return tab[(index >= 0 && index < kChConfigs) ? index : 0];
 }
 
 void config_name(const ChConfig& c, char* name, size_t len) {
     if (c.pipe >= 2)
-        snprintf(name, len, "rhs_warps%d%s_ychunk%d_pipe_regtab%s_xchunk%d", c.rhs_warps,
+        snprintf(name, len, "rhs_warps%d%s_ychunk%d_pipe_regtab%s_xchunk%d%s", c.rhs_warps,
                  c.rhs_split == 2 ? "_2pass_pipe" : (c.rhs_split ? "_2pass" : ""),
-                 c.y_chunk, c.pipe == 3 ? "_xy" : "", c.x_chunk);
+                 c.y_chunk, c.pipe == 3 ? "_xy" : "", c.x_chunk, c.ysplit ? "_ysplit" : "");
     else
         snprintf(name, len, "rhs_warps%d_ychunk%d%s", c.rhs_warps, c.y_chunk, c.pipe ? "_pipe" : "");
 }
@@ -1322,6 +1500,17 @@ cudaError_t launch_ch_step(const ChConfig& c, bool rhs_fp32, const GridDev* grid
     if (c.pipe) {
         // 64-100 registers and 8-17 KB of shared memory per one-warp CTA: up to 32 CTAs per SM
         const int gp = std::max(1, std::min(n_rows, sms * 32));
+        if (c.ysplit) {   // x sweep, x correction, y recurrences, update (register-table sweeps, 8-row y batches)
+            if (c.x_chunk == 8) ch_xsolve_pipe_rt_kernel<8><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+            else ch_xsolve_pipe_rt_kernel<16><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            ch_xcorr_kernel<<<n_rhs, 256, 0, s>>>(grids, items_rhs);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            ch_ysolve_split_kernel<8><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, parity, counters + 2);
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            ch_update_kernel<<<n_rhs, 256, 0, s>>>(grids, items_rhs, parity);
+            return cudaGetLastError();
+        }
         if (c.pipe >= 2 && c.x_chunk == 8)
             ch_xsolve_pipe_rt_kernel<8><<<gp, BLK, 0, s>>>(grids, items_rows, n_rows, counters + 1);
         else if (c.pipe >= 2)
@@ -1723,7 +1912,7 @@ int custen_ch_batch_step(void* h, int steps, int use_graph) {
     if (!b || steps < 0) return ch_fail_arg("invalid arguments");
     cudaSetDevice(b->device);
     int left = steps;
-    const int per_step = 3 + (batch_config(b).rhs_split ? 1 : 0);   // kernel launches in one step
+    const int per_step = ch_launches_per_step(batch_config(b));   // kernel launches in one step
     if (use_graph && left >= 2) {
         int st = capture_pairs(b);
         if (st) return st;

@@ -233,7 +233,7 @@ unsigned long long custen_ch_batch_launches(void* batch);
  * the fields, and keeps the fastest; results do not depend on it. No reference counterpart. */
 int custen_ch_batch_autotune(void* batch, int steps, char* name, size_t len);
 int custen_ch_batch_config(void* batch, char* name, size_t len);
-int custen_ch_batch_set_config(void* batch, int index);   /* 0 .. 20; -1: the default */
+int custen_ch_batch_set_config(void* batch, int index);   /* 0 .. 21; -1: the default */
 /* Checkpoint / resume of one grid through an HDF5 snapshot (the format below): save writes "c" = cCurr,
  * "c_old" = cOld and "t" = time; load takes "c" (must be n x n), "c_old" if present (else cCurr, as the
  * reference starts) and returns "t" in *time (NaN when absent, as in the reference's own snapshots).

@@ -81,7 +81,7 @@ def main() -> int:
     # CH batch, every kernel configuration
     sizes = [64, 160, 96]
     c0 = [np.random.default_rng(60 + k).uniform(-0.1, 0.1, (n, n)) for k, n in enumerate(sizes)]
-    for cfg in range(21):
+    for cfg in range(22):
         b = cs.CahnHilliardBatch(sizes)
         b.set_config(cfg)
         for k, c in enumerate(c0):

@@ -153,7 +153,7 @@ def test_fp32_stencil_variant_error_reported(gpu, n, steps):
     b.close()
 
 
-CH_CONFIGS = 21
+CH_CONFIGS = 22
 
 
 def test_fp32_variant_configurations_identical(gpu):
