@@ -1672,7 +1672,13 @@ struct Batch {
     unsigned long long launches = 0;
 };
 
-static ChConfig batch_config(const Batch* b) { return ch_config(b->cfg < 0 ? kChBatchDefault : b->cfg); }
+// The default: configuration 20, or with fewer 32-line warps than FP64 sub-partitions (4 per SM) its split
+// y sweep (configuration 21), which a warp's FP64 instruction count bounds there (a 2048^2 grid alone: 1.32
+// against 1.87 ms per step). Both compute the same values.
+static ChConfig batch_config(const Batch* b) {
+    if (b->cfg >= 0) return ch_config(b->cfg);
+    return ch_config(b->n_items_rows < 4 * b->sms ? kChSplitConfig : kChBatchDefault);
+}
 
 static thread_local std::string g_ch_err;
 static int ch_fail(cudaError_t e, const char* what) {
