@@ -24,7 +24,7 @@ struct GridDev {
 
 // Table layout for one n (m = n - 2), all double:
 //   [0, m) ds  [m, 2m) dl  [2m, 3m) rd = 1/diag  [3m, 4m) du  [4m, 5m) dw   (factored, zero-padded:
-//   ds[0] = ds[1] = dl[0] = 0, du[m-1] = 0, dw[m-2] = dw[m-1] = 0; ds and dl stored multiplied by rd)
+//   ds[0] = ds[1] = dl[0] = 0, du[m-1] = 0, dw[m-2] = dw[m-1] = 0)
 //   [5m, 6m) inv1  [6m, 7m) inv2   border columns of the cyclic correction
 //   [7m, 7m+4) omega  [7m+4, 7m+8) a, b, d, e  [7m+8, 7m+33) linear 5x5 weights  [7m+33, 7m+42) the
 //   non-linear 3x3 weights

@@ -401,8 +401,9 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
                 const double a_s = __shfl_sync(FULL, tds, k), a_l = __shfl_sync(FULL, tdl, k);
                 const double a_r = __shfl_sync(FULL, trd, k);
                 if (i < m) {
-                    // scaled multipliers (table: ds / pivot, dl / pivot): one dependent FMA per element
-                    double t = fma(-a_l, b1, fma(-a_s, b2, x * a_r));
+                    double t = fma(-a_s, b2, x);
+                    t = fma(-a_l, b1, t);
+                    t *= a_r;
                     b2 = b1;
                     b1 = t;
                     blk[lane][k] = t;
@@ -436,7 +437,8 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_kernel(const GridDev* __restric
                 const int i = cx + k;
                 const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
                 if (i < m) {
-                    double y = fma(-a_u, f1, fma(-a_w, f2, blk[lane][k]));   // f2 term off the chain
+                    double y = fma(-a_u, f1, blk[lane][k]);
+                    y = fma(-a_w, f2, y);
                     f2 = f1;
                     f1 = y;
                     blk[lane][k] = y;
@@ -530,8 +532,9 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
                 const double a_r = __shfl_sync(FULL, trd, k);
                 const double val = corr ? fma(-cx1, c2, fma(-cx2, c1, v[k])) : v[k];
                 if (y < m) {
-                    // scaled multipliers (table: ds / pivot, dl / pivot): one dependent FMA per element
-                    double w = fma(-a_l, b1, fma(-a_s, b2, val * a_r));
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
                     b2 = b1;
                     b1 = w;
                     v[k] = w;
@@ -559,7 +562,8 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_kernel(const GridDev* __restric
                 const int y = yb + k;
                 const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
                 if (y < m) {
-                    double w = fma(-a_u, f1, fma(-a_w, f2, v[k]));   // f2 term off the chain
+                    double w = fma(-a_u, f1, v[k]);
+                    w = fma(-a_w, f2, w);
                     f2 = f1;
                     f1 = w;
                     v[k] = w;
@@ -688,8 +692,9 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_pipe_kernel(const GridDev* __re
                 const double a_s = __shfl_sync(FULL, tds, k), a_l = __shfl_sync(FULL, tdl, k);
                 const double a_r = __shfl_sync(FULL, trd, k);
                 if (i < m) {
-                    // scaled multipliers (table: ds / pivot, dl / pivot): one dependent FMA per element
-                    double t = fma(-a_l, b1, fma(-a_s, b2, x * a_r));
+                    double t = fma(-a_s, b2, x);
+                    t = fma(-a_l, b1, t);
+                    t *= a_r;
                     b2 = b1;
                     b1 = t;
                     blk[b][lane][k] = t;
@@ -726,7 +731,8 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_pipe_kernel(const GridDev* __re
                 const int i = cx + k;
                 const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
                 if (i < m) {
-                    double y = fma(-a_u, f1, fma(-a_w, f2, blk[b][lane][k]));   // f2 term off the chain
+                    double y = fma(-a_u, f1, blk[b][lane][k]);
+                    y = fma(-a_w, f2, y);
                     f2 = f1;
                     f1 = y;
                     blk[b][lane][k] = y;
@@ -825,8 +831,9 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_pipe_rt_kernel(const GridDev* _
                 const int i = cx + k;
                 const double x = blk[b][lane][k];
                 if (i < m) {
-                    // scaled multipliers (table: ds / pivot, dl / pivot): one dependent FMA per element
-                    double t = fma(-tl[k], b1, fma(-ts[k], b2, x * tr[k]));
+                    double t = fma(-ts[k], b2, x);
+                    t = fma(-tl[k], b1, t);
+                    t *= tr[k];
                     b2 = b1;
                     b1 = t;
                     blk[b][lane][k] = t;
@@ -862,7 +869,8 @@ __global__ void __launch_bounds__(BLK) ch_xsolve_pipe_rt_kernel(const GridDev* _
             for (int k = XC - 1; k >= 0; --k) {
                 const int i = cx + k;
                 if (i < m) {
-                    double y = fma(-tu[k], f1, fma(-tw[k], f2, blk[b][lane][k]));   // f2 term off the chain
+                    double y = fma(-tu[k], f1, blk[b][lane][k]);
+                    y = fma(-tw[k], f2, y);
                     f2 = f1;
                     f1 = y;
                     blk[b][lane][k] = y;
@@ -971,8 +979,9 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_pipe_kernel(const GridDev* __re
                 const double vk = vb[b][k][lane];
                 const double val = corr ? fma(-cx1, c2, fma(-cx2, c1, vk)) : vk;
                 if (y < m) {
-                    // scaled multipliers (table: ds / pivot, dl / pivot): one dependent FMA per element
-                    double w = fma(-a_l, b1, fma(-a_s, b2, val * a_r));
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
                     b2 = b1;
                     b1 = w;
                     if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
@@ -1005,7 +1014,8 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_pipe_kernel(const GridDev* __re
                 const int y = yb + k;
                 const double a_u = __shfl_sync(FULL, tdu, k), a_w = __shfl_sync(FULL, tdw, k);
                 if (y < m) {
-                    double w = fma(-a_u, f1, fma(-a_w, f2, vb[b][k][lane]));   // f2 term off the chain
+                    double w = fma(-a_u, f1, vb[b][k][lane]);
+                    w = fma(-a_w, f2, w);
                     f2 = f1;
                     f1 = w;
                     if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
@@ -1125,8 +1135,9 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_pipe_rt_kernel(const GridDev* _
                 const double vk = vb[b][k][lane];
                 const double val = corr ? fma(-cx1, c2, fma(-cx2, c1, vk)) : vk;
                 if (y < m) {
-                    // scaled multipliers (table: ds / pivot, dl / pivot): one dependent FMA per element
-                    double w = fma(-a_l, b1, fma(-a_s, b2, val * a_r));
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
                     b2 = b1;
                     b1 = w;
                     if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
@@ -1160,7 +1171,8 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_pipe_rt_kernel(const GridDev* _
                 const int y = yb + k;
                 const double a_u = tu[k], a_w = tw[k];
                 if (y < m) {
-                    double w = fma(-a_u, f1, fma(-a_w, f2, vb[b][k][lane]));   // f2 term off the chain
+                    double w = fma(-a_u, f1, vb[b][k][lane]);
+                    w = fma(-a_w, f2, w);
                     f2 = f1;
                     f1 = w;
                     if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
@@ -1325,8 +1337,9 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_split_kernel(const GridDev* __r
                 const double vk = vb[b][k][lane];
                 const double val = vk;   // corrected by ch_xcorr_kernel
                 if (y < m) {
-                    // scaled multipliers (table: ds / pivot, dl / pivot): one dependent FMA per element
-                    double w = fma(-a_l, b1, fma(-a_s, b2, val * a_r));
+                    double w = fma(-a_s, b2, val);
+                    w = fma(-a_l, b1, w);
+                    w *= a_r;
                     b2 = b1;
                     b1 = w;
                     if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
@@ -1360,7 +1373,8 @@ __global__ void __launch_bounds__(BLK) ch_ysolve_split_kernel(const GridDev* __r
                 const int y = yb + k;
                 const double a_u = tu[k], a_w = tw[k];
                 if (y < m) {
-                    double w = fma(-a_u, f1, fma(-a_w, f2, vb[b][k][lane]));   // f2 term off the chain
+                    double w = fma(-a_u, f1, vb[b][k][lane]);
+                    w = fma(-a_w, f2, w);
                     f2 = f1;
                     f1 = w;
                     if (in_bounds((long long)y * n + x, 0, (long long)n * n)) t[(size_t)y * n + x] = w;
@@ -1607,11 +1621,9 @@ static void fill_table(double* t, double* work, int n, double lx, double gamma, 
     const double det = 1.0 / (y11 * y22 - y21 * y12);
     for (int k = 0; k < tab_size(n); ++k) t[k] = 0.0;
     for (int i = 0; i < m; ++i) {
-        // the forward sweeps multiply the right-hand side by the reciprocal pivot first and take the
-        // multipliers already divided by it, so that one FMA per element depends on the previous one
+        t[i] = (i > 1) ? ds[i] : 0.0;
+        t[m + i] = (i > 0) ? dl[i] : 0.0;
         t[2 * m + i] = 1.0 / dg[i];
-        t[i] = (i > 1) ? ds[i] * t[2 * m + i] : 0.0;
-        t[m + i] = (i > 0) ? dl[i] * t[2 * m + i] : 0.0;
         t[3 * m + i] = (i < m - 1) ? du[i] : 0.0;
         t[4 * m + i] = (i < m - 2) ? dw[i] : 0.0;
         t[5 * m + i] = inv1[i];
