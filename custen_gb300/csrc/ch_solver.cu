@@ -21,8 +21,9 @@
 //                           x sweep's rank-2 correction as it reads, then cNew = cBar + delta written
 //                           over cOld (the two field buffers swap roles every step).
 // Each kernel is persistent over a work list that covers all grids (largest first, claimed through
-// an atomic counter), so grids of different sizes share one launch. A step is three launches; pairs
-// of steps are captured in a CUDA graph.
+// an atomic counter), so grids of different sizes share one launch. A step is three launches (four with
+// the two-pass right-hand side, six with the split y sweep as well); pairs of steps are captured in a CUDA
+// graph.
 //
 // The sweeps come in three forms, all computing the same values (ChConfig, tuned per batch):
 // staged through registers (the kernels K2/K3 below), pipelined (the next chunk copied into shared
